@@ -1,0 +1,296 @@
+"""ctypes binding of libaccx.so (include/accx.h).
+
+This is plumbing for tests, the bench and Python users: every call goes straight
+to the C ABI, which runs the sm_103a kernels.  There is no Python or CPU
+fallback: if the shared library is missing the import raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libaccx.so")
+
+OK = 0
+ERR_INVALID_ARG, ERR_CUDA, ERR_OOM, ERR_SELF_LOOP, ERR_UNSORTED, ERR_RANGE, ERR_ASYMMETRIC, ERR_IO, \
+    ERR_TOO_LARGE, ERR_NOT_READY, ERR_TIMEOUT, ERR_ADMISSION, ERR_NO_DEVICE = range(-1, -14, -1)
+
+GRAPH_VALIDATE = 1
+GEN_RMAT, GEN_ER, GEN_CHUNG_LU = 0, 1, 2
+KIND_MERGE, KIND_GALLOP, KIND_BITMAP = 0, 1, 2
+KIND_NAMES = ("merge", "gallop", "bitmap")
+POLICY_HEURISTIC, POLICY_TABLE, POLICY_MERGE, POLICY_GALLOP, POLICY_BITMAP, POLICY_MODEL = range(6)
+POLICIES = {"heuristic": POLICY_HEURISTIC, "table": POLICY_TABLE, "merge": POLICY_MERGE,
+            "gallop": POLICY_GALLOP, "bitmap": POLICY_BITMAP, "model": POLICY_MODEL}
+NB = 24
+PHASES = ("plan", "merge", "gallop", "bitmap", "mirror")
+UNCLASSIFIED, CORE, HUB = 0, 1, 2
+
+
+class AccxError(RuntimeError):
+    def __init__(self, status, what=""):
+        self.status = status
+        super().__init__("%s: %s (%d)" % (what, strerror(status), status))
+
+
+class GenParams(C.Structure):
+    _fields_ = [("kind", C.c_int), ("p0", C.c_uint64), ("p1", C.c_uint64), ("q0", C.c_double),
+                ("q1", C.c_double), ("q2", C.c_double), ("seed", C.c_uint64)]
+
+
+class CountOpts(C.Structure):
+    _fields_ = [("policy", C.c_int), ("table", C.POINTER(C.c_uint8)), ("bias", C.c_int32),
+                ("block_warps", C.c_int), ("bitmap_window_kb", C.c_int), ("timing", C.c_int)]
+
+
+class ScanSummary(C.Structure):
+    _fields_ = [("cores", C.c_uint32), ("clusters", C.c_uint32), ("hubs", C.c_uint32), ("outliers", C.c_uint32),
+                ("similar_entries", C.c_uint64), ("noncore_pairs", C.c_uint64)]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libaccx.so not built (run __graft_entry__.build()): %s" % LIB_PATH)
+    lib = C.CDLL(LIB_PATH)
+    P = C.c_void_p
+    sigs = {
+        "accx_strerror": (C.c_char_p, [C.c_int]),
+        "accx_version": (C.c_char_p, []),
+        "accx_graph_create": (C.c_int, [P, P, C.c_uint32, C.c_uint64, C.c_uint, P, C.POINTER(P)]),
+        "accx_graph_load_dir": (C.c_int, [C.c_char_p, C.c_uint, P, C.POINTER(P)]),
+        "accx_graph_free": (C.c_int, [P]),
+        "accx_graph_size": (C.c_int, [P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint64)]),
+        "accx_graph_download": (C.c_int, [P, P, P, P]),
+        "accx_graph_device_ptrs": (C.c_int, [P, C.POINTER(P), C.POINTER(P), C.POINTER(P)]),
+        "accx_graph_generate": (C.c_int, [C.POINTER(GenParams), P, C.POINTER(P)]),
+        "accx_generate_host": (C.c_int, [C.POINTER(GenParams), C.POINTER(C.c_uint32), C.POINTER(C.c_uint64), P, P]),
+        "accx_write_graph_dir": (C.c_int, [C.c_char_p, P, P, C.c_uint32, C.c_uint64]),
+        "accx_cn_count": (C.c_int, [P, C.POINTER(CountOpts), P, P]),
+        "accx_cn_last_stats": (C.c_int, [P, P, P]),
+        "accx_cn_last_owner_work": (C.c_int, [P, P]),
+        "accx_cn_last_timings": (C.c_int, [P, P]),
+        "accx_scan_query": (C.c_int, [P, C.c_double, C.c_int, P, P, P, C.POINTER(ScanSummary), P]),
+        "accx_scan_pairs": (C.c_int, [P, P, C.c_uint64, C.POINTER(C.c_uint64), P]),
+        "accx_eps_string": (C.c_int, [C.c_double, C.c_char_p, C.c_size_t]),
+        "accx_write_result": (C.c_int, [P, C.c_char_p, C.c_double, C.c_int, P]),
+        "accx_similar_exact": (C.c_int, [C.c_uint32, C.c_uint32, C.c_uint32, C.c_double]),
+        "accx_similar_exact_batch": (C.c_int, [C.c_uint64, P, P, P, C.c_double, P]),
+    }
+    for name, (res, args) in sigs.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    return lib
+
+
+lib = _load()
+
+
+def strerror(status):
+    return lib.accx_strerror(int(status)).decode()
+
+
+def version():
+    return lib.accx_version().decode()
+
+
+def _check(status, what):
+    if status != OK:
+        raise AccxError(status, what)
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def gen_params(kind, p0, p1, q0=0.0, q1=0.0, q2=0.0, seed=1):
+    return GenParams(kind, p0, p1, q0, q1, q2, seed)
+
+
+def rmat_params(scale, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=1):
+    return gen_params(GEN_RMAT, scale, edge_factor, a, b, c, seed)
+
+
+def er_params(n, mean_degree, seed=1):
+    return gen_params(GEN_ER, n, int(n * mean_degree // 2), seed=seed)
+
+
+def chung_lu_params(n, mean_degree, gamma=2.1, max_degree=1e6, seed=1):
+    return gen_params(GEN_CHUNG_LU, n, int(n * mean_degree // 2), gamma, max_degree, seed=seed)
+
+
+def generate_host(params):
+    """Host generator (same graph as Graph.generate); returns (off uint32[n+1], dst int32[m])."""
+    n = C.c_uint32()
+    m = C.c_uint64()
+    _check(lib.accx_generate_host(C.byref(params), C.byref(n), C.byref(m), None, None), "generate_host")
+    off = np.zeros(n.value + 1, np.uint32)
+    dst = np.zeros(max(m.value, 1), np.int32)
+    _check(lib.accx_generate_host(C.byref(params), C.byref(n), C.byref(m), _ptr(off), _ptr(dst)), "generate_host")
+    return off, dst[:m.value]
+
+
+def write_graph_dir(path, off, dst):
+    off = np.ascontiguousarray(off, np.uint32)
+    dst = np.ascontiguousarray(dst, np.int32)
+    _check(lib.accx_write_graph_dir(path.encode(), _ptr(off), _ptr(dst), len(off) - 1, len(dst)), "write_graph_dir")
+
+
+def eps_string(eps):
+    buf = C.create_string_buffer(512)
+    _check(lib.accx_eps_string(float(eps), buf, 512), "eps_string")
+    return buf.value.decode()
+
+
+def similar_exact(cnn, du, dv, eps):
+    return bool(lib.accx_similar_exact(int(cnn), int(du), int(dv), float(eps)))
+
+
+def similar_exact_batch(cnn, du, dv, eps):
+    cnn = np.ascontiguousarray(cnn, np.uint32)
+    du = np.ascontiguousarray(du, np.uint32)
+    dv = np.ascontiguousarray(dv, np.uint32)
+    out = np.zeros(max(len(cnn), 1), np.uint8)
+    _check(lib.accx_similar_exact_batch(len(cnn), _ptr(cnn), _ptr(du), _ptr(dv), float(eps), _ptr(out)),
+           "similar_exact_batch")
+    return out[:len(cnn)].astype(bool)
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return C.c_void_p(stream)
+    return C.c_void_p(int(stream.cuda_stream))  # a torch.cuda.Stream
+
+
+class Graph:
+    """A device-resident CSR graph handle (accx_graph)."""
+
+    def __init__(self, handle):
+        self._h = handle
+        n = C.c_uint32()
+        m = C.c_uint64()
+        _check(lib.accx_graph_size(self._h, C.byref(n), C.byref(m)), "graph_size")
+        self.n, self.m = int(n.value), int(m.value)
+
+    @classmethod
+    def from_csr(cls, off, dst, validate=True, stream=None):
+        off = np.ascontiguousarray(off, np.uint32)
+        dst = np.ascontiguousarray(dst, np.int32)
+        h = C.c_void_p()
+        _check(lib.accx_graph_create(_ptr(off), _ptr(dst) if len(dst) else None, len(off) - 1, len(dst),
+                                     GRAPH_VALIDATE if validate else 0, _stream_ptr(stream), C.byref(h)),
+               "graph_create")
+        return cls(h)
+
+    @classmethod
+    def from_device(cls, off_ptr, dst_ptr, n, m, validate=True, stream=None):
+        h = C.c_void_p()
+        _check(lib.accx_graph_create(C.c_void_p(off_ptr), C.c_void_p(dst_ptr), n, m,
+                                     GRAPH_VALIDATE if validate else 0, _stream_ptr(stream), C.byref(h)),
+               "graph_create")
+        return cls(h)
+
+    @classmethod
+    def load_dir(cls, path, validate=True, stream=None):
+        h = C.c_void_p()
+        _check(lib.accx_graph_load_dir(path.encode(), GRAPH_VALIDATE if validate else 0, _stream_ptr(stream),
+                                       C.byref(h)), "graph_load_dir")
+        return cls(h)
+
+    @classmethod
+    def generate(cls, params, stream=None):
+        h = C.c_void_p()
+        _check(lib.accx_graph_generate(C.byref(params), _stream_ptr(stream), C.byref(h)), "graph_generate")
+        return cls(h)
+
+    def free(self):
+        if self._h:
+            lib.accx_graph_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def download(self, stream=None):
+        off = np.zeros(self.n + 1, np.uint32)
+        dst = np.zeros(max(self.m, 1), np.int32)
+        _check(lib.accx_graph_download(self._h, _ptr(off), _ptr(dst), _stream_ptr(stream)), "graph_download")
+        return off, dst[:self.m]
+
+    def device_ptrs(self):
+        o, d, c = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        _check(lib.accx_graph_device_ptrs(self._h, C.byref(o), C.byref(d), C.byref(c)), "device_ptrs")
+        return o.value, d.value, c.value
+
+    @staticmethod
+    def _opts(policy, table, bias, block_warps, window_kb, timing=False):
+        pol = POLICIES[policy] if isinstance(policy, str) else int(policy)
+        tab = None
+        keep = None
+        if table is not None:
+            keep = np.ascontiguousarray(table, np.uint8).reshape(-1)
+            assert keep.size == NB * NB
+            tab = keep.ctypes.data_as(C.POINTER(C.c_uint8))
+            if pol == POLICY_HEURISTIC and isinstance(policy, str) and policy == "heuristic":
+                pass
+        return CountOpts(pol, tab, int(bias), int(block_warps), int(window_kb), 1 if timing else 0), keep
+
+    def count(self, policy="heuristic", table=None, bias=0, out="host", block_warps=0, window_kb=0, stream=None,
+              timing=False):
+        """All-edge CN counts.  out="host" returns an int32 numpy array; out=None
+        leaves them resident; out=<int device pointer> copies there."""
+        opts, keep = self._opts(policy, table, bias, block_warps, window_kb, timing)
+        if out == "host":
+            res = np.zeros(max(self.m, 1), np.int32)
+            _check(lib.accx_cn_count(self._h, C.byref(opts), _ptr(res), _stream_ptr(stream)), "cn_count")
+            return res[:self.m]
+        target = None if out is None else C.c_void_p(out)
+        _check(lib.accx_cn_count(self._h, C.byref(opts), target, _stream_ptr(stream)), "cn_count")
+        del keep
+        return None
+
+    def last_stats(self):
+        e = np.zeros(3, np.uint64)
+        w = np.zeros(3, np.uint64)
+        _check(lib.accx_cn_last_stats(self._h, _ptr(e), _ptr(w)), "cn_last_stats")
+        return {KIND_NAMES[k]: {"edges": int(e[k]), "work": int(w[k])} for k in range(3)}
+
+    def owner_work(self):
+        w = np.zeros(3, np.uint64)
+        _check(lib.accx_cn_last_owner_work(self._h, _ptr(w)), "cn_last_owner_work")
+        return {KIND_NAMES[k]: int(w[k]) for k in range(3)}
+
+    def timings(self):
+        """Milliseconds per phase (plan, merge, gallop, bitmap, mirror) of the last timed count."""
+        ms = np.zeros(5, np.float32)
+        _check(lib.accx_cn_last_timings(self._h, _ptr(ms)), "cn_last_timings")
+        return dict(zip(PHASES, (float(x) for x in ms)))
+
+    def scan(self, eps, mu, want_sim=True, want_label=True, want_cluster=True, stream=None):
+        sim = np.zeros(max(self.m, 1), np.uint8) if want_sim else None
+        lab = np.zeros(max(self.n, 1), np.int32) if want_label else None
+        cl = np.zeros(max(self.n, 1), np.int32) if want_cluster else None
+        s = ScanSummary()
+        _check(lib.accx_scan_query(self._h, float(eps), int(mu), _ptr(sim), _ptr(lab), _ptr(cl), C.byref(s),
+                                   _stream_ptr(stream)), "scan_query")
+        return {"sim": None if sim is None else sim[:self.m], "label": None if lab is None else lab[:self.n],
+                "cluster": None if cl is None else cl[:self.n], "summary": s.as_dict()}
+
+    def pairs(self, stream=None):
+        k = C.c_uint64()
+        _check(lib.accx_scan_pairs(self._h, None, 0, C.byref(k), _stream_ptr(stream)), "scan_pairs")
+        out = np.zeros(2 * max(k.value, 1), np.int32)
+        _check(lib.accx_scan_pairs(self._h, _ptr(out), k.value, C.byref(k), _stream_ptr(stream)), "scan_pairs")
+        return out[:2 * k.value].reshape(-1, 2)
+
+    def write_result(self, path, eps, mu, stream=None):
+        _check(lib.accx_write_result(self._h, path.encode(), float(eps), int(mu), _stream_ptr(stream)), "write_result")

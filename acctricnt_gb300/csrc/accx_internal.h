@@ -1,0 +1,97 @@
+// Internal definitions shared by the libaccx translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include "../../include/accx.h"
+
+#define ACCX_VERSION_STR "accx 0.1 sm_103a"
+
+// Device arrays are padded by this many int32 so that 16-byte vector loads of
+// a list's last window never leave the allocation.
+#define ACCX_DST_PAD 64
+
+// Bitmap-kernel work item: owner u, its CSR entry range [e0, e1).
+struct accx_bitmap_item {
+  uint32_t u, e0, e1, pad;
+};
+
+struct accx_graph {
+  int device = 0;
+  uint32_t n = 0;
+  uint64_t m = 0;
+  uint32_t *d_off = nullptr;  // n+1
+  int32_t *d_dst = nullptr;   // m + ACCX_DST_PAD
+  int32_t *d_cnt = nullptr;   // m
+  int32_t cnt_bias = 0;
+  bool cnt_valid = false;
+
+  // counting scratch
+  uint2 *d_edge_list = nullptr;  // m/2+1 owned entries: merge items from the front, gallop from the back
+  accx_bitmap_item *d_items = nullptr;
+  uint64_t items_cap = 0;
+  unsigned long long *d_counters = nullptr;  // [0] merge, [1] gallop, [2] bitmap items, [3..5] work per kind
+  uint64_t stats_edges[ACCX_NUM_KINDS] = {0, 0, 0};
+  uint64_t stats_work[ACCX_NUM_KINDS] = {0, 0, 0};
+  uint8_t *d_table = nullptr;  // ACCX_NB*ACCX_NB kinds
+  cudaEvent_t ev[ACCX_NUM_PHASES + 1] = {};
+  bool timed = false;
+
+  // SCAN query state
+  uint32_t *d_simbits = nullptr;  // ceil(m/32) words
+  int32_t *d_core_count = nullptr;
+  int32_t *d_label = nullptr;
+  int32_t *d_parent = nullptr;
+  int32_t *d_hubmin = nullptr;
+  int32_t *d_hubmax = nullptr;
+  unsigned long long *d_qcounters = nullptr;  // query counters
+  bool query_valid = false;
+  double last_eps = 0;
+  int last_mu = 0;
+  // pairs of the last query (built on demand)
+  unsigned long long *d_pairs = nullptr;
+  unsigned long long *d_pairs_tmp = nullptr;
+  uint64_t pairs_cap = 0;
+  uint64_t npairs = 0;
+  bool pairs_valid = false;
+  accx_scan_summary summary{};
+
+  // trained cost model state (accx_model_*)
+  void *model = nullptr;
+};
+
+#define ACCX_CUDA_TRY(call)                                   \
+  do {                                                        \
+    cudaError_t _e = (call);                                  \
+    if (_e != cudaSuccess) {                                  \
+      accx_set_cuda_error(_e, #call, __FILE__, __LINE__);     \
+      return (_e == cudaErrorMemoryAllocation) ? ACCX_ERR_OOM \
+                                               : ACCX_ERR_CUDA; \
+    }                                                         \
+  } while (0)
+
+void accx_set_cuda_error(cudaError_t e, const char *what, const char *file, int line);
+
+// True when p is a device (or managed) pointer.
+bool accx_is_device_ptr(const void *p);
+
+// Copies between host/device buffers chosen by pointer kind.
+int accx_copy_out(void *dst, const void *dev_src, size_t bytes, cudaStream_t s);
+int accx_copy_in(void *dev_dst, const void *src, size_t bytes, cudaStream_t s);
+
+// Grid for a grid-stride kernel: enough CTAs to fill every SM `per_sm` times.
+int accx_grid_for(int device, int block, int per_sm);
+int accx_sm_count(int device);
+
+// Internal: creates a handle around device arrays already owned by it.
+int accx_graph_validate_device(accx_graph *g, int full, cudaStream_t s);
+int accx_ensure_count_scratch(accx_graph *g);
+
+// Cost-model state attached to a handle (model.cu).
+void accx_model_release(accx_graph *g);
+int accx_model_table(accx_graph *g, uint8_t *table);
+
+// Exclusive/inclusive helpers implemented in gen.cu.
+int accx_build_csr_from_keys(accx_graph *g, unsigned long long *d_keys, uint64_t nkeys, uint32_t n,
+                             cudaStream_t s);

@@ -1,0 +1,316 @@
+// Graph handles: upload, file loading, validation, download; status strings.
+//
+// Replaces the reference's Graph loader (scan-query-cuda/util/graph.cu:33-214):
+// the same b_degree.bin / b_adj.bin format and the same input checks
+// (CheckInputGraph: no self loops, strictly increasing rows), plus a range and a
+// symmetry check the reference leaves implicit, run as one GPU pass.  Arrays live
+// in plain device memory for the handle's lifetime instead of managed memory.
+#include <errno.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "accx_internal.h"
+#include "devutil.cuh"
+
+static thread_local char g_last_cuda_error[512];
+
+void accx_set_cuda_error(cudaError_t e, const char *what, const char *file, int line) {
+  snprintf(g_last_cuda_error, sizeof(g_last_cuda_error), "%s at %s:%d: %s", cudaGetErrorString(e), file, line,
+           what);
+  if (getenv("ACCX_DEBUG")) fprintf(stderr, "[accx] CUDA error %s\n", g_last_cuda_error);
+}
+
+extern "C" const char *accx_strerror(int status) {
+  switch (status) {
+    case ACCX_OK: return "ok";
+    case ACCX_ERR_INVALID_ARG: return "invalid argument";
+    case ACCX_ERR_CUDA: return g_last_cuda_error[0] ? g_last_cuda_error : "CUDA error";
+    case ACCX_ERR_OOM: return "out of memory";
+    case ACCX_ERR_SELF_LOOP: return "Self loop";
+    case ACCX_ERR_UNSORTED: return "Edges not sorted in increasing id order!";
+    case ACCX_ERR_RANGE: return "neighbour id or offsets out of range";
+    case ACCX_ERR_ASYMMETRIC: return "graph is not symmetric";
+    case ACCX_ERR_IO: return "file cannot be read or written";
+    case ACCX_ERR_TOO_LARGE: return "size beyond the supported maximum";
+    case ACCX_ERR_NOT_READY: return "not ready";
+    case ACCX_ERR_TIMEOUT: return "bounded device wait timed out";
+    case ACCX_ERR_ADMISSION: return "request exceeds the HBM budget";
+    case ACCX_ERR_NO_DEVICE: return "no CUDA device";
+    default: return "unknown status";
+  }
+}
+
+extern "C" const char *accx_version(void) { return ACCX_VERSION_STR; }
+
+bool accx_is_device_ptr(const void *p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+int accx_copy_out(void *dst, const void *dev_src, size_t bytes, cudaStream_t s) {
+  if (!bytes) return ACCX_OK;
+  ACCX_CUDA_TRY(cudaMemcpyAsync(dst, dev_src, bytes, cudaMemcpyDefault, s));
+  if (!accx_is_device_ptr(dst)) ACCX_CUDA_TRY(cudaStreamSynchronize(s));
+  return ACCX_OK;
+}
+
+int accx_copy_in(void *dev_dst, const void *src, size_t bytes, cudaStream_t s) {
+  if (!bytes) return ACCX_OK;
+  ACCX_CUDA_TRY(cudaMemcpyAsync(dev_dst, src, bytes, cudaMemcpyDefault, s));
+  if (!accx_is_device_ptr(src)) ACCX_CUDA_TRY(cudaStreamSynchronize(s));
+  return ACCX_OK;
+}
+
+int accx_sm_count(int device) {
+  static int cached[64] = {0};
+  if (device < 0 || device >= 64) return 1;
+  if (!cached[device]) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || v <= 0) v = 1;
+    cached[device] = v;
+  }
+  return cached[device];
+}
+
+int accx_grid_for(int device, int block, int per_sm) {
+  (void)block;
+  return accx_sm_count(device) * per_sm;
+}
+
+// ---------------------------------------------------------------------------
+// Validation: one thread per entry sets a bit per kind of defect; the host
+// reports them in the reference's order (range, self loop, order), then symmetry.
+#define V_RANGE 1
+#define V_SELF 2
+#define V_UNSORTED 4
+#define V_ASYM 8
+// Range checks always run (every kernel indexes off[] with neighbour ids); the
+// order, self-loop and symmetry checks run when `full` is set.
+__global__ void k_validate(const uint32_t *__restrict__ off, const int32_t *__restrict__ dst, uint32_t n,
+                           uint32_t m, int full, int *__restrict__ status) {
+  __shared__ accx_tile_rows<256> sh;
+  uint32_t base = blockIdx.x * 256u;
+  uint32_t e = base + threadIdx.x;
+  uint32_t u = accx_tile_row<256>(off, n, m, base, e, &sh);
+  if (e >= m) return;
+  int32_t v = dst[e];
+  if (v < 0 || (uint32_t)v >= n) { atomicOr(status, V_RANGE); return; }
+  if (!full) return;
+  if ((uint32_t)v == u) { atomicOr(status, V_SELF); return; }
+  if (e > off[u] && dst[e - 1] >= v) { atomicOr(status, V_UNSORTED); return; }
+  uint32_t b = off[v], t = off[v + 1];
+  uint32_t r = accx_lower_bound(dst, b, t, (int32_t)u);
+  if (r >= t || dst[r] != (int32_t)u) atomicOr(status, V_ASYM);
+}
+
+static int check_offsets_host(const uint32_t *off, uint32_t n, uint64_t m) {
+  if (off[0] != 0 || off[n] != m) return ACCX_ERR_RANGE;
+  for (uint32_t i = 0; i < n; i++)
+    if (off[i + 1] < off[i]) return ACCX_ERR_RANGE;
+  return ACCX_OK;
+}
+
+__global__ void k_check_offsets(const uint32_t *__restrict__ off, uint32_t n, uint32_t m, int *status) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (off[i + 1] < off[i]) atomicOr(status, V_RANGE);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0 && (off[0] != 0 || off[n] != m)) atomicOr(status, V_RANGE);
+}
+
+int accx_graph_validate_device(accx_graph *g, int full, cudaStream_t s) {
+  int *d_status = nullptr;
+  ACCX_CUDA_TRY(cudaMalloc(&d_status, sizeof(int)));
+  int zero = 0;
+  int rc = ACCX_OK;
+  do {
+    if (cudaMemcpyAsync(d_status, &zero, sizeof(int), cudaMemcpyHostToDevice, s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
+    k_check_offsets<<<accx_grid_for(g->device, 256, 4), 256, 0, s>>>(g->d_off, g->n, (uint32_t)g->m, d_status);
+    int st = 0;
+    if (cudaMemcpyAsync(&st, d_status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
+    if (st) { rc = ACCX_ERR_RANGE; break; }
+    if (g->m) {
+      uint32_t blocks = (uint32_t)((g->m + 255) / 256);
+      k_validate<<<blocks, 256, 0, s>>>(g->d_off, g->d_dst, g->n, (uint32_t)g->m, full, d_status);
+      if (cudaMemcpyAsync(&st, d_status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+          cudaStreamSynchronize(s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
+      rc = (st & V_RANGE) ? ACCX_ERR_RANGE : (st & V_SELF) ? ACCX_ERR_SELF_LOOP
+         : (st & V_UNSORTED) ? ACCX_ERR_UNSORTED : (st & V_ASYM) ? ACCX_ERR_ASYMMETRIC : ACCX_OK;
+    }
+  } while (0);
+  cudaFree(d_status);
+  if (rc == ACCX_ERR_CUDA) accx_set_cuda_error(cudaGetLastError(), "validate", __FILE__, __LINE__);
+  return rc;
+}
+
+static int alloc_graph(uint32_t n, uint64_t m, accx_graph **out) {
+  if (m >= (1ull << 32) - ACCX_DST_PAD) return ACCX_ERR_TOO_LARGE;
+  int dev = 0;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return ACCX_ERR_NO_DEVICE;
+  }
+  ACCX_CUDA_TRY(cudaGetDevice(&dev));
+  accx_graph *g = new (std::nothrow) accx_graph();
+  if (!g) return ACCX_ERR_OOM;
+  g->device = dev;
+  g->n = n;
+  g->m = m;
+  if (cudaMalloc(&g->d_off, sizeof(uint32_t) * ((size_t)n + 1)) != cudaSuccess ||
+      cudaMalloc(&g->d_dst, sizeof(int32_t) * ((size_t)m + ACCX_DST_PAD)) != cudaSuccess) {
+    cudaGetLastError();
+    accx_graph_free(g);
+    return ACCX_ERR_OOM;
+  }
+  // The padding reads as ids that match nothing.
+  if (cudaMemset(g->d_dst + m, 0xff, sizeof(int32_t) * ACCX_DST_PAD) != cudaSuccess) {
+    accx_graph_free(g);
+    return ACCX_ERR_CUDA;
+  }
+  *out = g;
+  return ACCX_OK;
+}
+
+extern "C" int accx_graph_create(const uint32_t *off, const int32_t *dst, uint32_t n, uint64_t m, unsigned flags,
+                                 void *stream, accx_graph **out) {
+  if (!off || (!dst && m) || !out) return ACCX_ERR_INVALID_ARG;
+  *out = nullptr;
+  cudaStream_t s = (cudaStream_t)stream;
+  bool off_dev = accx_is_device_ptr(off);
+  if (!off_dev) {
+    int rc = check_offsets_host(off, n, m);
+    if (rc) return rc;
+  }
+  accx_graph *g = nullptr;
+  int rc = alloc_graph(n, m, &g);
+  if (rc) return rc;
+  rc = accx_copy_in(g->d_off, off, sizeof(uint32_t) * ((size_t)n + 1), s);
+  if (!rc) rc = accx_copy_in(g->d_dst, dst, sizeof(int32_t) * (size_t)m, s);
+  if (!rc) rc = accx_graph_validate_device(g, (flags & ACCX_GRAPH_VALIDATE) ? 1 : 0, s);
+  if (!rc) {
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) { accx_set_cuda_error(e, "create", __FILE__, __LINE__); rc = ACCX_ERR_CUDA; }
+  }
+  if (rc) { accx_graph_free(g); return rc; }
+  *out = g;
+  return ACCX_OK;
+}
+
+extern "C" int accx_graph_load_dir(const char *dir, unsigned flags, void *stream, accx_graph **out) {
+  if (!dir || !out) return ACCX_ERR_INVALID_ARG;
+  *out = nullptr;
+  std::string d(dir);
+  FILE *f = fopen((d + "/b_degree.bin").c_str(), "rb");
+  if (!f) return ACCX_ERR_IO;
+  int32_t int_size = 0;
+  uint32_t n = 0, m = 0;
+  if (fread(&int_size, 4, 1, f) != 1 || fread(&n, 4, 1, f) != 1 || fread(&m, 4, 1, f) != 1) {
+    fclose(f);
+    return ACCX_ERR_IO;
+  }
+  std::vector<uint32_t> off((size_t)n + 1);
+  std::vector<int32_t> deg(n);
+  size_t got = n ? fread(deg.data(), 4, n, f) : 0;
+  fclose(f);
+  if (got != n) return ACCX_ERR_IO;
+  uint64_t acc = 0;
+  off[0] = 0;
+  for (uint32_t i = 0; i < n; i++) {
+    if (deg[i] < 0) return ACCX_ERR_RANGE;
+    acc += (uint32_t)deg[i];
+    if (acc > m) return ACCX_ERR_RANGE;
+    off[i + 1] = (uint32_t)acc;
+  }
+  if (acc != m) return ACCX_ERR_RANGE;
+  f = fopen((d + "/b_adj.bin").c_str(), "rb");
+  if (!f) return ACCX_ERR_IO;
+  int32_t *h_dst = nullptr;
+  if (cudaMallocHost(&h_dst, sizeof(int32_t) * ((size_t)m + 1)) != cudaSuccess) {
+    cudaGetLastError();
+    fclose(f);
+    return ACCX_ERR_OOM;
+  }
+  got = m ? fread(h_dst, 4, m, f) : 0;
+  fclose(f);
+  int rc = (got == m) ? ACCX_OK : ACCX_ERR_IO;
+  if (!rc) rc = accx_graph_create(off.data(), h_dst, n, m, flags, stream, out);
+  cudaFreeHost(h_dst);
+  return rc;
+}
+
+extern "C" int accx_graph_free(accx_graph *g) {
+  if (!g) return ACCX_ERR_INVALID_ARG;
+  void *ptrs[] = {g->d_off,       g->d_dst,   g->d_cnt,       g->d_edge_list, g->d_items,
+                  g->d_counters,  g->d_table, g->d_simbits,   g->d_core_count, g->d_label,
+                  g->d_parent,    g->d_hubmin, g->d_hubmax,   g->d_qcounters,  g->d_pairs,
+                  g->d_pairs_tmp};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  for (int i = 0; i <= ACCX_NUM_PHASES; i++)
+    if (g->ev[i]) cudaEventDestroy(g->ev[i]);
+  accx_model_release(g);
+  delete g;
+  return ACCX_OK;
+}
+
+extern "C" int accx_graph_size(const accx_graph *g, uint32_t *n, uint64_t *m) {
+  if (!g) return ACCX_ERR_INVALID_ARG;
+  if (n) *n = g->n;
+  if (m) *m = g->m;
+  return ACCX_OK;
+}
+
+extern "C" int accx_graph_download(const accx_graph *g, uint32_t *off, int32_t *dst, void *stream) {
+  if (!g) return ACCX_ERR_INVALID_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (off) {
+    int rc = accx_copy_out(off, g->d_off, sizeof(uint32_t) * ((size_t)g->n + 1), s);
+    if (rc) return rc;
+  }
+  if (dst) {
+    int rc = accx_copy_out(dst, g->d_dst, sizeof(int32_t) * (size_t)g->m, s);
+    if (rc) return rc;
+  }
+  return ACCX_OK;
+}
+
+extern "C" int accx_graph_device_ptrs(const accx_graph *g, const uint32_t **off, const int32_t **dst,
+                                      const int32_t **cnt) {
+  if (!g) return ACCX_ERR_INVALID_ARG;
+  if (off) *off = g->d_off;
+  if (dst) *dst = g->d_dst;
+  if (cnt) *cnt = g->cnt_valid ? g->d_cnt : nullptr;
+  return ACCX_OK;
+}
+
+extern "C" int accx_write_graph_dir(const char *dir, const uint32_t *off, const int32_t *dst, uint32_t n,
+                                    uint64_t m) {
+  if (!dir || !off || (!dst && m)) return ACCX_ERR_INVALID_ARG;
+  if (m >= (1ull << 32)) return ACCX_ERR_TOO_LARGE;
+  std::string d(dir);
+  FILE *f = fopen((d + "/b_degree.bin").c_str(), "wb");
+  if (!f) return ACCX_ERR_IO;
+  int32_t int_size = 4;
+  uint32_t n32 = n, m32 = (uint32_t)m;
+  bool ok = fwrite(&int_size, 4, 1, f) == 1 && fwrite(&n32, 4, 1, f) == 1 && fwrite(&m32, 4, 1, f) == 1;
+  std::vector<int32_t> deg(n);
+  for (uint32_t i = 0; i < n; i++) deg[i] = (int32_t)(off[i + 1] - off[i]);
+  if (n) ok = ok && fwrite(deg.data(), 4, n, f) == n;
+  ok = (fclose(f) == 0) && ok;
+  if (!ok) return ACCX_ERR_IO;
+  f = fopen((d + "/b_adj.bin").c_str(), "wb");
+  if (!f) return ACCX_ERR_IO;
+  ok = m ? fwrite(dst, 4, m, f) == m : true;
+  ok = (fclose(f) == 0) && ok;
+  return ok ? ACCX_OK : ACCX_ERR_IO;
+}

@@ -1,0 +1,388 @@
+"""Benchmark: all-edge common-neighbour counting + SCAN queries on one GB300.
+
+Workload (one step = one full all-edge CN count of the resident graph):
+R-MAT scale 24, edge factor 16, (a,b,c,d) = (0.57, 0.19, 0.19, 0.05), seed 1,
+symmetrised, self loops and duplicates removed, generated on the device.  The
+count is timed for the scheduled policy (the headline `value`) and for the
+plain fixed-heuristic policy (the reference's ratio-50 merge/galloping rule) on
+the same GPU; SCAN queries at eps in {0.2, 0.5, 0.8}, mu = 5 report p50/p99.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+N > 1 runs independent replicas (one graph per rank, seed + rank): the path has
+no exchange step, so there is no collective on the data path.  --impl reference
+times the reference algorithm's CPU implementation (the oracle port of
+CheckCoreBitmap, all host threads) on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "learned-sched vs plain all-edge CN Gedges/s (bit-exact); SCAN p50/p99 ms"
+UNIT = "Gedges/s"
+QUERY_EPS = (0.2, 0.5, 0.8)
+QUERY_MU = 5
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--scale", type=int, default=24)
+    ap.add_argument("--edge-factor", type=int, default=16)
+    ap.add_argument("--policy", default="auto", help="scheduled policy: auto (trained model) or a fixed one")
+    ap.add_argument("--query-reps", type=int, default=20)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup(args):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench_%d.csv" % os.getpid())
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc:
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                p = [x.strip() for x in line.split(",")]
+                if len(p) < 9:
+                    continue
+                try:
+                    sm.append(float(p[1]))
+                    mx.append(float(p[2]))
+                except ValueError:
+                    continue
+                for nm, val in zip(names, p[5:9]):
+                    if val.lower() == "active":
+                        reasons.add(nm)
+        except OSError:
+            return None
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def pick_policy(G, args):
+    """The scheduled policy: the trained cost model when available, else the
+    fixed policy given on the command line."""
+    if args.policy != "auto":
+        return args.policy, None
+    try:
+        from acctricnt_gb300 import sched
+        table, info = sched.schedule_for(G)
+        return "table", (table, info)
+    except Exception as e:  # no model yet: report the best fixed policy instead
+        return "bitmap", {"note": "cost model unavailable: %s" % e}
+
+
+def time_counts(G, policy, table, steps, warmup, stream, world, timing=True):
+    import torch
+    for _ in range(warmup):
+        G.count(policy=policy, table=table, out=None, stream=stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    phases = {}
+    ev0.record(stream)
+    for _ in range(steps):
+        G.count(policy=policy, table=table, out=None, stream=stream, timing=timing)
+        if timing:
+            for k, v in G.timings().items():
+                phases[k] = phases.get(k, 0.0) + v
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / steps
+    return ms, {k: v / steps for k, v in phases.items()}
+
+
+def measure_queries(G, reps):
+    lat = []
+    for eps in QUERY_EPS:
+        G.scan(eps, QUERY_MU, want_sim=False, want_label=False, want_cluster=False)  # warm
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            G.scan(eps, QUERY_MU, want_sim=False, want_label=False, want_cluster=False)
+            lat.append((time.perf_counter() - t0) * 1e3)
+    lat.sort()
+    p = lambda q: lat[min(len(lat) - 1, int(round(q * (len(lat) - 1))))]
+    return {"p50_ms": round(p(0.50), 3), "p99_ms": round(p(0.99), 3), "n": len(lat),
+            "eps": list(QUERY_EPS), "mu": QUERY_MU}
+
+
+def measure_e2e(G, policy, table, reps):
+    """Through the C ABI with host buffers: pinned host CSR -> accx_graph_create
+    (copy + validation) -> count -> counts copied back to pinned host memory."""
+    import torch
+    from acctricnt_gb300 import accx
+    off, dst = G.download()
+    t_off = torch.from_numpy(off.view(np.int32)).pin_memory()
+    t_dst = torch.from_numpy(dst).pin_memory()
+    t_cnt = torch.empty(G.m, dtype=torch.int32).pin_memory()
+    times = []
+    for i in range(reps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        H = accx.Graph.from_device(t_off.data_ptr(), t_dst.data_ptr(), G.n, G.m, validate=True)
+        H.count(policy=policy, table=table, out=t_cnt.data_ptr())
+        H.free()
+        dt = time.perf_counter() - t0
+        if i:
+            times.append(dt)
+    t = statistics.median(times)
+    return {"value": round(G.m / t / 1e9, 4), "unit": UNIT, "h2d_bytes_per_step": 4 * (G.n + 1) + 4 * G.m,
+            "d2h_bytes_per_step": 4 * G.m, "ms_per_step": round(t * 1e3, 3),
+            "path": "accx_graph_create(host pinned CSR, validate) + accx_cn_count(host pinned out)"}
+
+
+def cpu_baseline(off, dst, budget_s, nthreads):
+    """Oracle port of CheckCoreBitmap on a stride sample of owner vertices."""
+    from oracle import oracle
+    n = len(off) - 1
+    cnn = np.full(len(dst), 2, np.int32)
+    stride = 4096
+    while True:
+        owners = np.arange(0, n, stride, dtype=np.uint32)
+        t0 = time.perf_counter()
+        k, _ = oracle.cn_count_owners(off, dst, owners, nthreads, cnn)
+        dt = time.perf_counter() - t0
+        if dt > budget_s / 4 or stride == 1:
+            break
+        stride = max(1, int(stride * max(dt, 1e-3) / budget_s * 2))
+        stride = max(1, stride)
+    return {"value": round(2 * k / dt / 1e9, 5), "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": "owner vertices 0, %d, 2*%d, ... (%d of %d), their %d owned edges (%d CSR entries) "
+                      "in %.2f s" % (stride, stride, len(owners), n, k, 2 * k, dt)}
+
+
+def alg_bytes(G, dominant, stats, owner_work):
+    """Algorithmic bytes of one launch of the dominant phase."""
+    if dominant == "bitmap":
+        e = stats["bitmap"]["edges"]
+        return 4 * stats["bitmap"]["work"] + 4 * owner_work["bitmap"] + 8 * e
+    if dominant == "merge":
+        return 4 * stats["merge"]["work"] + 4 * owner_work["merge"] + 12 * stats["merge"]["edges"]
+    if dominant == "gallop":
+        return 4 * stats["gallop"]["work"] + 12 * stats["gallop"]["edges"]
+    if dominant == "mirror":
+        return 4 * 4 * G.m
+    return 8 * G.m
+
+
+def run_gb300(args):
+    import torch
+    from acctricnt_gb300 import accx
+    rank, world, local = dist_setup(args)
+    G = accx.Graph.generate(accx.rmat_params(args.scale, args.edge_factor, seed=1 + rank))
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    policy, sched_info = pick_policy(G, args)
+    table = sched_info[0] if isinstance(sched_info, tuple) else None
+    # correctness guard: the scheduled and plain counts are identical
+    G.count(policy=policy, table=table, out=None, stream=sp)
+    a = G.count(policy=policy, table=table, stream=sp)
+    b = G.count(policy="heuristic", stream=sp)
+    bit_exact = bool(np.array_equal(a, b))
+    del a, b
+    with ClockSampler(local) as clk:
+        ms, phases = time_counts(G, policy, table, args.steps, args.warmup, sp, world)
+    ms = max_over_ranks(ms, world)
+    stats = G.last_stats()
+    owner_work = G.owner_work()
+    plain_ms, plain_phases = time_counts(G, "heuristic", None, args.steps, args.warmup, sp, world)
+    plain_ms = max_over_ranks(plain_ms, world)
+    total_m = sum_over_ranks(G.m, world)
+    value = total_m / (ms / 1e3) / 1e9
+    plain_value = total_m / (plain_ms / 1e3) / 1e9
+    G.count(policy=policy, table=table, out=None, stream=sp)
+    torch.cuda.synchronize()
+    scan = measure_queries(G, args.query_reps)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    dominant = max(("merge", "gallop", "bitmap", "mirror", "plan"), key=lambda k: phases.get(k, 0.0))
+    dom_ms = phases.get(dominant, 0.0)
+    ab = alg_bytes(G, dominant, stats, owner_work)
+    achieved = ab / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else None
+    traffic = None
+    try:
+        tr = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
+        traffic = tr.get(dominant)
+    except Exception:
+        pass
+    roofline = {"bound": "hbm", "kernel": "k_" + dominant, "achieved": round(achieved, 1) if achieved else None,
+                "peak": peak, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback",
+                "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None, "traffic": traffic,
+                "alg_bytes_per_launch": int(ab), "launch_ms": round(dom_ms, 3),
+                "merge_equiv_bytes": int(4 * float(np.sum(np.diff(G.download()[0]).astype(np.float64) ** 2)) + 4 * G.m)}
+    e2e = None
+    if not args.no_e2e and rank == 0:
+        e2e = measure_e2e(G, policy, table, 2)
+    cpu = None
+    if not args.no_cpu and rank == 0 and world == 1:
+        off, dst = G.download()
+        cpu = cpu_baseline(off, dst, args.cpu_seconds, os.cpu_count() or 1)
+    line = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": "R-MAT scale %d, edge factor %d, (0.57,0.19,0.19,0.05), seed 1+rank; all-edge CN "
+                                   "count; SCAN eps %s mu %d" % (args.scale, args.edge_factor, list(QUERY_EPS), QUERY_MU),
+                       "n": G.n, "m": G.m, "policy": policy, "parallelism": "replicas%d" % world,
+                       "l2": "inputs larger than L2 (CSR %.2f GB, counts %.2f GB)" % ((4 * G.m + 4 * G.n) / 1e9,
+                                                                                   4 * G.m / 1e9)},
+            "plain": {"policy": "heuristic", "value": round(plain_value, 4), "ms_per_step": round(plain_ms, 3),
+                      "phases_ms": {k: round(v, 3) for k, v in plain_phases.items()}},
+            "speedup_vs_plain": round(plain_ms / ms, 3), "bit_exact_vs_plain": bit_exact,
+            "phases_ms": {k: round(v, 3) for k, v in phases.items()}, "kinds": stats,
+            "scan": scan, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": 6 * args.steps, "clocks": clk.summary(),
+            "sched": sched_info[1] if isinstance(sched_info, tuple) else sched_info}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_reference(args):
+    """The reference algorithm's CPU implementation on the host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from acctricnt_gb300 import accx
+    from oracle import oracle
+    G = accx.Graph.generate(accx.rmat_params(args.scale, args.edge_factor, seed=1))
+    off, dst = G.download()
+    G.free()
+    n = len(off) - 1
+    threads = os.cpu_count() or 1
+    cnn = np.full(len(dst), 2, np.int32)
+    # each step: a stride sample of owners sized to about budget/steps seconds
+    stride = 8192
+    owners = np.arange(0, n, stride, dtype=np.uint32)
+    t0 = time.perf_counter()
+    oracle.cn_count_owners(off, dst, owners, threads, cnn)
+    dt = max(time.perf_counter() - t0, 1e-3)
+    per_step = max(1.0, args.cpu_seconds / max(1, args.steps + args.warmup))
+    stride = max(1, int(stride * dt / per_step))
+    rates = []
+    total_k = 0
+    total_t = 0.0
+    for i in range(args.warmup + args.steps):
+        owners = np.arange(i % stride, n, stride, dtype=np.uint32)
+        t0 = time.perf_counter()
+        k, _ = oracle.cn_count_owners(off, dst, owners, threads, cnn)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            total_k += k
+            total_t += dt
+            rates.append(2 * k / dt / 1e9)
+    value = 2 * total_k / total_t / 1e9
+    line = {"metric": METRIC, "value": round(value, 5), "unit": UNIT, "impl": "reference", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_t / args.steps * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": "R-MAT scale %d, edge factor %d, (0.57,0.19,0.19,0.05), seed 1; all-edge CN count"
+                                   % (args.scale, args.edge_factor), "n": n, "m": int(len(dst))},
+            "cpu_baseline": {"value": round(value, 5), "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "per step: owner vertices i, i+%d, ... of %d (CheckCoreBitmap restated in "
+                                       "C, OpenMP, all host threads)" % (stride, n)},
+            "e2e": {"value": round(value, 5), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,203 @@
+/*
+ * accx.h -- C ABI of the GB300-native all-edge common-neighbour (CN) counter and
+ * SCAN structural-clustering query (libaccx.so).
+ *
+ * Every function returns ACCX_OK (0) or a negative status (see accx_strerror);
+ * nothing in the library calls exit() or traps.  Pointers are plain host or
+ * device pointers; "stream" is a cudaStream_t passed as void* (NULL = the legacy
+ * default stream).  A graph handle is not thread-safe: use one handle per thread,
+ * or serialise calls on it.
+ *
+ * Reference interfaces replaced (paths inside the AccTriCnt tree):
+ *   accx_graph_create / accx_graph_load_dir
+ *       Graph::Graph, ReadDegree, ReadAdjacencyList, CheckInputGraph
+ *       (scan-query-cuda/util/graph.cu:33-51, :53-70, :76-194, :196-214)
+ *   accx_cn_count
+ *       SCAN_XP::CheckCore (scan-query-cuda/experimental_scan_xp_multigpu_multipass.cu:3-166):
+ *       kernels set_intersection_GPU_bitmap_warp_per_vertex, _shared_merge_filtered,
+ *       _shared_galloping_filtered (scan-query-cuda/scan_xp_multi_gpu_multi_pass_common.cu:32-495)
+ *       and the reverse-offset mirror (PostComputeCoreChecking, scan-query-cuda/scan_xp_common.cu:220-237)
+ *   accx_scan_query
+ *       PostComputeCoreChecking similarity/core part (scan_xp_common.cu:239-267),
+ *       ClusterCore (:73-85), LabelNonCore/CheckHub (:87-111), PostProcess (:113-135),
+ *       MarkClusterMinEleAsId (:137-158)
+ *   accx_scan_pairs / accx_write_result
+ *       PrepareResultOutput (scan_xp_common.cu:160-199) and Graph::Output (util/graph.cu:216-245)
+ */
+#ifndef ACCX_H
+#define ACCX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------- */
+#define ACCX_OK 0
+#define ACCX_ERR_INVALID_ARG (-1)   /* NULL handle/pointer, bad size or option */
+#define ACCX_ERR_CUDA (-2)          /* a CUDA runtime call failed */
+#define ACCX_ERR_OOM (-3)           /* device or host allocation failed */
+#define ACCX_ERR_SELF_LOOP (-4)     /* input has an entry (u,u) */
+#define ACCX_ERR_UNSORTED (-5)      /* a neighbour list is not strictly increasing */
+#define ACCX_ERR_RANGE (-6)         /* a neighbour id >= n, or offsets inconsistent */
+#define ACCX_ERR_ASYMMETRIC (-7)    /* (u,v) present without (v,u) */
+#define ACCX_ERR_IO (-8)            /* a graph or result file cannot be read/written */
+#define ACCX_ERR_TOO_LARGE (-9)     /* sizes beyond the format (m >= 2^32) or a stated limit */
+#define ACCX_ERR_NOT_READY (-10)    /* counts not computed yet, or request still running */
+#define ACCX_ERR_TIMEOUT (-11)      /* a bounded device wait gave up */
+#define ACCX_ERR_ADMISSION (-12)    /* a request does not fit the server's HBM budget */
+#define ACCX_ERR_NO_DEVICE (-13)    /* no CUDA device visible */
+
+const char *accx_strerror(int status);
+
+/* Library build identification ("accx <version> sm_103a"). */
+const char *accx_version(void);
+
+/* ---- graphs ---------------------------------------------------------------- */
+typedef struct accx_graph accx_graph;
+
+/* Flags for accx_graph_create. */
+#define ACCX_GRAPH_VALIDATE 1u       /* check self loops, order, range, symmetry on the GPU */
+
+/* Copies a CSR (off[n+1], dst[m], host or device pointers -- detected with
+ * cudaPointerGetAttributes) to device memory and returns a handle.  dst holds
+ * sorted neighbour ids without self loops, as the reference's b_adj.bin. */
+int accx_graph_create(const uint32_t *off, const int32_t *dst, uint32_t n, uint64_t m, unsigned flags,
+                      void *stream, accx_graph **out);
+
+/* Reads <dir>/b_degree.bin and <dir>/b_adj.bin (the reference format: int32
+ * int_size, uint32 n, uint32 m, int32 degree[n]; int32 dst[m]) straight into a
+ * handle.  Validates like Graph::CheckInputGraph. */
+int accx_graph_load_dir(const char *dir, unsigned flags, void *stream, accx_graph **out);
+
+int accx_graph_free(accx_graph *g);
+int accx_graph_size(const accx_graph *g, uint32_t *n, uint64_t *m);
+
+/* Copies the CSR back (host or device destination pointers). */
+int accx_graph_download(const accx_graph *g, uint32_t *off, int32_t *dst, void *stream);
+
+/* Device pointers of the resident arrays (off[n+1], dst[m padded], cnt[m] or
+ * NULL before the first count).  Valid until accx_graph_free. */
+int accx_graph_device_ptrs(const accx_graph *g, const uint32_t **off, const int32_t **dst, const int32_t **cnt);
+
+/* Device-side synthetic generators (seeded, counter-based: the same seed gives the
+ * same graph on any GPU and on the host generator below).  The edge stream is
+ * symmetrised; self loops and duplicate edges are removed; lists are sorted. */
+#define ACCX_GEN_RMAT 0      /* p0 = scale, p1 = edge factor, a,b,c in q0..q2 */
+#define ACCX_GEN_ER 1        /* p0 = n, p1 = undirected edge draws (n*mean/2) */
+#define ACCX_GEN_CHUNG_LU 2  /* p0 = n, p1 = edge draws, q0 = gamma, q1 = max expected degree */
+typedef struct {
+  int kind;
+  uint64_t p0, p1;
+  double q0, q1, q2;
+  uint64_t seed;
+} accx_gen_params;
+
+int accx_graph_generate(const accx_gen_params *params, void *stream, accx_graph **out);
+
+/* Host generator with the same output, for tests and for files.  Two calls:
+ * with off/dst NULL it returns the sizes; then fill caller buffers of n+1 / m. */
+int accx_generate_host(const accx_gen_params *params, uint32_t *n, uint64_t *m, uint32_t *off, int32_t *dst);
+
+/* Writes a CSR in the reference's b_degree.bin / b_adj.bin format. */
+int accx_write_graph_dir(const char *dir, const uint32_t *off, const int32_t *dst, uint32_t n, uint64_t m);
+
+/* ---- all-edge CN counting ---------------------------------------------------- */
+/* Kernel kinds a policy can assign to a degree bucket. */
+#define ACCX_KIND_MERGE 0   /* warp merge-path over uint4-vectorised windows */
+#define ACCX_KIND_GALLOP 1  /* per-element binary search of the small list in the large one */
+#define ACCX_KIND_BITMAP 2  /* per-owner shared-memory bitmap over id windows, ballot/popc probe */
+#define ACCX_NUM_KINDS 3
+
+/* Policies. */
+#define ACCX_POLICY_HEURISTIC 0 /* reference rule: gallop iff d_max/50 > d_min, else merge */
+#define ACCX_POLICY_TABLE 1     /* per-bucket kinds from `table` (ACCX_NB x ACCX_NB bytes) */
+#define ACCX_POLICY_MERGE 2     /* every edge by one kind ... */
+#define ACCX_POLICY_GALLOP 3
+#define ACCX_POLICY_BITMAP 4
+#define ACCX_POLICY_MODEL 5     /* the handle's trained cost model (accx_model_*) picks per bucket */
+
+/* Degree buckets: b(d) = min(floor(log2 d), ACCX_NB-1) for d >= 1.  An edge's
+ * bucket is (b(d_owner), b(d_other)); the owner is the endpoint with the larger
+ * degree (ties: smaller id), as in the reference CPU bitmap build. */
+#define ACCX_NB 24
+
+typedef struct {
+  int policy;
+  const uint8_t *table;   /* ACCX_NB*ACCX_NB kinds, row = owner bucket; for ACCX_POLICY_TABLE */
+  int32_t bias;           /* added to every count; 2 gives the reference's common_node_num */
+  int block_warps;        /* bitmap/merge CTA size in warps (0 = tuned default) */
+  int bitmap_window_kb;   /* shared-memory bitmap window in KiB (0 = tuned default) */
+  int timing;             /* 1: record CUDA events around each phase (accx_cn_last_timings) */
+} accx_count_opts;
+
+/* Counts cnt[e] = |N(u) ∩ N(v)| + bias for every CSR entry e=(u,v) into the
+ * handle's resident count array, then (if out != NULL) copies it to `out` (host
+ * or device).  opts NULL = heuristic policy, bias 0. */
+int accx_cn_count(accx_graph *g, const accx_count_opts *opts, int32_t *out, void *stream);
+
+/* Per-kind statistics of the last accx_cn_count: edges[k] owned edges and
+ * work[k] probe elements assigned to kind k. */
+int accx_cn_last_stats(const accx_graph *g, uint64_t edges[ACCX_NUM_KINDS], uint64_t work[ACCX_NUM_KINDS]);
+
+/* Owner-side elements per kind of the last count: sum of owner degrees over the
+ * merge/gallop edges, and the owner lists the bitmap kernel staged (per work item). */
+int accx_cn_last_owner_work(const accx_graph *g, uint64_t owner_work[ACCX_NUM_KINDS]);
+
+/* Phases timed when accx_count_opts.timing is set. */
+#define ACCX_PHASE_PLAN 0    /* classify + bitmap work items */
+#define ACCX_PHASE_MERGE 1
+#define ACCX_PHASE_GALLOP 2
+#define ACCX_PHASE_BITMAP 3
+#define ACCX_PHASE_MIRROR 4
+#define ACCX_NUM_PHASES 5
+/* Milliseconds per phase of the last timed count (waits for it to finish). */
+int accx_cn_last_timings(const accx_graph *g, float ms[ACCX_NUM_PHASES]);
+
+/* ---- SCAN query ------------------------------------------------------------- */
+#define ACCX_UNCLASSIFIED 0
+#define ACCX_CORE 1
+#define ACCX_HUB 2
+
+typedef struct {
+  uint32_t cores, clusters, hubs, outliers; /* PostProcess counts */
+  uint64_t similar_entries;                 /* entries with sim = 1 */
+  uint64_t noncore_pairs;                   /* unique (cluster, non-core) pairs */
+} accx_scan_summary;
+
+/* Runs the SCAN query on the resident counts (accx_cn_count must have run with
+ * any bias; the bias is taken into account).  Outputs are optional (NULL =
+ * skip, host or device pointers): sim[m] (0/1 bytes), label[n] (0/1/2),
+ * cluster[n] (minimum vertex id of the core's cluster, -1 for non-cores). */
+int accx_scan_query(accx_graph *g, double eps, int mu, uint8_t *sim, int32_t *label, int32_t *cluster,
+                    accx_scan_summary *summary, void *stream);
+
+/* The sorted unique (cluster id, non-core vertex) pairs of the last query, as
+ * pairs[2k] = cluster id, pairs[2k+1] = vertex; cap = capacity in pairs.  Returns
+ * the count in *npairs (ACCX_ERR_TOO_LARGE when cap is short, *npairs still set). */
+int accx_scan_pairs(accx_graph *g, int32_t *pairs, uint64_t cap, uint64_t *npairs, void *stream);
+
+/* The result-file name part for eps: std::to_string(eps) with trailing '0'/'u'
+ * characters removed (scan_xp_common.cu:191-192). */
+int accx_eps_string(double eps, char *out, size_t cap);
+
+/* Writes <dir>/scanxp-result-<eps>-<mu>.txt for the last query, byte-identical to
+ * the reference's Graph::Output. */
+int accx_write_result(accx_graph *g, const char *dir, double eps, int mu, void *stream);
+
+/* The exact similarity predicate for one entry, on the host: cnn = cnt + 2,
+ * du/dv = degree + 1.  Returns 1 when the reference's
+ * (double)((long double)cnn / sqrt((long double)du*dv)) >= eps, decided in
+ * exact integer arithmetic. */
+int accx_similar_exact(uint32_t cnn, uint32_t du, uint32_t dv, double eps);
+
+/* accx_similar_exact over k triples: out[i] = 0/1. */
+int accx_similar_exact_batch(uint64_t k, const uint32_t *cnn, const uint32_t *du, const uint32_t *dv, double eps,
+                             uint8_t *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ACCX_H */

@@ -1,0 +1,340 @@
+/*
+ * accx_oracle.c -- CPU restatement of the reference's all-edge common-neighbour
+ * count and SCAN query.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Nothing in the product library links or calls this
+ * file; only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load
+ * it, and only as the checker (or as the timed CPU baseline), never as a
+ * fallback.  Parity is pinned: tests/test_oracle_golden.py checks every function
+ * here against fixtures produced by the reference's own CPU build
+ * (scan-query, BIT_VEC variant) run through oracle/ref_harness.cpp.
+ *
+ * Reference files (paths inside the AccTriCnt tree):
+ *   scan-query/util/graph.cpp:126-221       b_degree.bin / b_adj.bin loader, input checks
+ *   scan-query/scan_xp.cpp:58-82            constructor: common_node_num[e] = 2, label = 0
+ *   scan-query/scan_xp.cpp:220-337          CheckCoreBitmap (degree-owner rule, bitmap probe,
+ *                                           symmetric assign by BinarySearch)
+ *   scan-query/scan_xp.cpp:112-141          CheckCoreCompSimCore (long double predicate, cores)
+ *   scan-query/scan_xp.cpp:1915-1955        ClusterCore, CheckHub, LabelNonCore
+ *   scan-query/scan_xp.cpp:1983-2074        MarkClusterMinEleAsId, PrepareResultOutput
+ *   scan-query/util/graph.cpp:254-294       Graph::Output (result file format)
+ *   scan-query/util/union_find.h:18-35      FindRoot / Union (larger root under smaller)
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define ORC_UNCLASSIFIED 0
+#define ORC_CORE 1
+#define ORC_HUB 2
+
+/* Input validation as in Graph::CheckInputGraph (graph.cpp:200-221):
+ * 0 = ok, -1 = self loop, -2 = a row not strictly increasing, -3 = id out of range. */
+int oracle_check_graph(uint32_t n, const uint32_t *off, const int32_t *dst) {
+  for (uint32_t i = 0; i < n; i++) {
+    for (uint32_t j = off[i]; j < off[i + 1]; j++) {
+      if (dst[j] < 0 || (uint32_t)dst[j] >= n) return -3;
+      if ((uint32_t)dst[j] == i) return -1;
+      if (j > off[i] && dst[j] <= dst[j - 1]) return -2;
+    }
+  }
+  return 0;
+}
+
+/* Recursive halving search for val inside dst[beg,end) (scan_xp.cpp:86-90); the
+ * caller guarantees val is present (the graph is symmetric). */
+static uint32_t orc_binary_search(const int32_t *a, uint32_t beg, uint32_t end, int32_t val) {
+  for (;;) {
+    uint32_t mid = (uint32_t)(((uint64_t)beg + end) / 2);
+    if (a[mid] == val) return mid;
+    if (val < a[mid]) end = mid; else beg = mid + 1;
+    if (beg >= end) return UINT32_MAX; /* not present: asymmetric input */
+  }
+}
+
+/* CheckCoreBitmap (scan_xp.cpp:220-337) with the original vertex order.
+ * cnn[e] = 2 + |N(u) ∩ N(v)| for every CSR entry.  The endpoint with the larger
+ * degree (ties: smaller id) owns the edge, probes the other endpoint's list
+ * against a bitmap of its own list, and mirrors the value to the reverse entry.
+ * Each owned edge is independent, so any thread count gives the same array.
+ * Returns 0, or -4 when the graph is not symmetric. */
+int oracle_cn_count(uint32_t n, const uint32_t *off, const int32_t *dst, int32_t *cnn, int nthreads) {
+  uint64_t m = off[n];
+  int bad = 0;
+  for (uint64_t e = 0; e < m; e++) cnn[e] = 2;
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel num_threads(nthreads) reduction(| : bad)
+#endif
+  {
+    uint8_t *bits = (uint8_t *)calloc(n ? n : 1, 1);
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 64)
+#endif
+    for (int64_t ui = 0; ui < (int64_t)n; ui++) {
+      uint32_t u = (uint32_t)ui;
+      uint32_t du = off[u + 1] - off[u];
+      int any_owned = 0;
+      for (uint32_t e = off[u]; e < off[u + 1]; e++) {
+        uint32_t v = (uint32_t)dst[e];
+        uint32_t dv = off[v + 1] - off[v];
+        if (du > dv || (du == dv && u < v)) { any_owned = 1; break; }
+      }
+      if (!any_owned) continue;
+      for (uint32_t e = off[u]; e < off[u + 1]; e++) bits[dst[e]] = 1;
+      for (uint32_t e = off[u]; e < off[u + 1]; e++) {
+        uint32_t v = (uint32_t)dst[e];
+        uint32_t dv = off[v + 1] - off[v];
+        if (!(du > dv || (du == dv && u < v))) continue;
+        int32_t c = 0;
+        for (uint32_t f = off[v]; f < off[v + 1]; f++) c += bits[dst[f]];
+        cnn[e] += c;
+        uint32_t r = orc_binary_search(dst, off[v], off[v + 1], (int32_t)u);
+        if (r == UINT32_MAX) { bad = 1; continue; }
+        cnn[r] = cnn[e];
+      }
+      for (uint32_t e = off[u]; e < off[u + 1]; e++) bits[dst[e]] = 0;
+    }
+    free(bits);
+  }
+  return bad ? -4 : 0;
+}
+
+/* CheckCoreCompSimCore (scan_xp.cpp:112-141): the similarity of entry e=(u,v) is
+ * (double)((long double)cnn[e] / sqrtl((long double)(d_u+1) * (d_v+1))) >= eps,
+ * computed in the host's long double exactly as the reference does.  core_count
+ * is accumulated per row (sequentially equal to the single-thread reference). */
+void oracle_similarity(uint32_t n, const uint32_t *off, const int32_t *dst, const int32_t *cnn, double eps,
+                       int mu, uint8_t *sim, int32_t *core_count, int32_t *label) {
+  for (uint32_t u = 0; u < n; u++) {
+    int32_t cc = 0;
+    for (uint32_t e = off[u]; e < off[u + 1]; e++) {
+      uint32_t v = (uint32_t)dst[e];
+      long double du = off[u + 1] - off[u] + 1;
+      long double dv = off[v + 1] - off[v] + 1;
+      double sim_value = (double)((long double)cnn[e] / sqrtl(du * dv));
+      if (sim_value >= eps) { cc++; sim[e] = 1; } else { sim[e] = 0; }
+    }
+    core_count[u] = cc;
+    label[u] = (cc >= mu) ? ORC_CORE : ORC_UNCLASSIFIED;
+  }
+}
+
+/* union_find.h:18-35, sequential: FindRoot with path compression; Union links the
+ * larger root under the smaller one, so a component's root is its minimum id. */
+static int32_t orc_find(int32_t *parent, int32_t x) {
+  int32_t r = x;
+  while (parent[r] != r) r = parent[r];
+  while (parent[x] != r) { int32_t nx = parent[x]; parent[x] = r; x = nx; }
+  return r;
+}
+static void orc_union(int32_t *parent, int32_t a, int32_t b) {
+  int32_t ra = orc_find(parent, a), rb = orc_find(parent, b);
+  if (ra == rb) return;
+  if (ra < rb) parent[rb] = ra; else parent[ra] = rb;
+}
+
+/* ClusterCore + LabelNonCore (scan_xp.cpp:1915-1955) and MarkClusterMinEleAsId
+ * (scan_xp.cpp:1983-2020) for the original order.  On return label[] holds
+ * 0/1/2 (UNCLASSIFIED/CORE/HUB) and cluster[u] holds the minimum vertex id of
+ * u's cluster for cores, -1 for non-cores. */
+void oracle_cluster(uint32_t n, const uint32_t *off, const int32_t *dst, const uint8_t *sim, int32_t *label,
+                    int32_t *cluster) {
+  int32_t *parent = (int32_t *)malloc(sizeof(int32_t) * (n ? n : 1));
+  for (uint32_t i = 0; i < n; i++) parent[i] = (int32_t)i;
+  for (uint32_t u = 0; u < n; u++) {
+    if (label[u] != ORC_CORE) continue;
+    for (uint32_t e = off[u]; e < off[u + 1]; e++) {
+      int32_t v = dst[e];
+      if (label[v] == ORC_CORE && sim[e]) orc_union(parent, (int32_t)u, v);
+    }
+  }
+  for (uint32_t u = 0; u < n; u++) {
+    if (label[u] == ORC_CORE) continue;
+    /* CheckHub: >= 2 distinct roots among core neighbours, similarity ignored. */
+    int32_t first = -1, hub = 0;
+    for (uint32_t e = off[u]; e < off[u + 1] && !hub; e++) {
+      int32_t v = dst[e];
+      if (label[v] != ORC_CORE) continue;
+      int32_t r = orc_find(parent, v);
+      if (first < 0) first = r; else if (r != first) hub = 1;
+    }
+    if (hub) label[u] = ORC_HUB;
+  }
+  /* The root of every component is its minimum id, which is also the cluster id
+   * MarkClusterMinEleAsId computes. */
+  for (uint32_t u = 0; u < n; u++) cluster[u] = (label[u] == ORC_CORE) ? orc_find(parent, (int32_t)u) : -1;
+  free(parent);
+}
+
+static int orc_pair_cmp(const void *a, const void *b) {
+  const int64_t x = *(const int64_t *)a, y = *(const int64_t *)b;
+  return (x > y) - (x < y);
+}
+
+/* PrepareResultOutput (scan_xp.cpp:2022-2074): the unique (cluster id, v) pairs of
+ * a core u, a non-core v and a similar entry (u,v), sorted by (cluster id, v).
+ * pairs[2k] = cluster id, pairs[2k+1] = v.  Returns the pair count; with
+ * pairs == NULL only counts candidate entries (an upper bound). */
+int64_t oracle_noncore_pairs(uint32_t n, const uint32_t *off, const int32_t *dst, const uint8_t *sim,
+                             const int32_t *label, const int32_t *cluster, int32_t *pairs) {
+  int64_t k = 0;
+  for (uint32_t u = 0; u < n; u++) {
+    if (label[u] != ORC_CORE) continue;
+    for (uint32_t e = off[u]; e < off[u + 1]; e++) {
+      int32_t v = dst[e];
+      if (label[v] != ORC_CORE && sim[e]) k++;
+    }
+  }
+  if (!pairs) return k;
+  int64_t *keys = (int64_t *)malloc(sizeof(int64_t) * (k ? k : 1));
+  int64_t j = 0;
+  for (uint32_t u = 0; u < n; u++) {
+    if (label[u] != ORC_CORE) continue;
+    for (uint32_t e = off[u]; e < off[u + 1]; e++) {
+      int32_t v = dst[e];
+      if (label[v] != ORC_CORE && sim[e]) keys[j++] = ((int64_t)cluster[u] << 32) | (uint32_t)v;
+    }
+  }
+  qsort(keys, (size_t)k, sizeof(int64_t), orc_pair_cmp);
+  int64_t w = 0;
+  for (int64_t i = 0; i < k; i++) {
+    if (i > 0 && keys[i] == keys[i - 1]) continue;
+    pairs[2 * w] = (int32_t)(keys[i] >> 32);
+    pairs[2 * w + 1] = (int32_t)(keys[i] & 0xffffffff);
+    w++;
+  }
+  free(keys);
+  return w;
+}
+
+/* The result-file name part for eps: std::to_string(eps) ("%f") with trailing
+ * '0' and 'u' characters erased (scan_xp.cpp:2062-2063). */
+void oracle_eps_string(double eps, char *out, int cap) {
+  char buf[512];
+  snprintf(buf, sizeof(buf), "%f", eps);
+  int len = (int)strlen(buf);
+  while (len > 0 && (buf[len - 1] == '0' || buf[len - 1] == 'u')) len--;
+  buf[len] = 0;
+  snprintf(out, (size_t)cap, "%s", buf);
+}
+
+/* Graph::Output (graph.cpp:254-294): writes <dir>/scanxp-result-<eps>-<mu>.txt.
+ * Returns 0 or -5 when the file cannot be opened. */
+int oracle_write_result(const char *dir, double eps, int mu, uint32_t n, const int32_t *label,
+                        const int32_t *cluster, const int32_t *pairs, int64_t npairs) {
+  char eps_s[512], path[4096];
+  oracle_eps_string(eps, eps_s, sizeof(eps_s));
+  snprintf(path, sizeof(path), "%s/scanxp-result-%s-%d.txt", dir, eps_s, mu);
+  FILE *f = fopen(path, "w");
+  if (!f) return -5;
+  fputs("c/n vertex_id cluster_id\n", f);
+  for (uint32_t i = 0; i < n; i++)
+    if (label[i] == ORC_CORE) fprintf(f, "c %u %d\n", i, cluster[i]);
+  for (int64_t k = 0; k < npairs; k++) fprintf(f, "n %d %d\n", pairs[2 * k + 1], pairs[2 * k]);
+  fclose(f);
+  return 0;
+}
+
+/* Reads b_degree.bin / b_adj.bin (graph.cpp:126-198).  *n_out and *m_out receive
+ * the header sizes; with off/dst NULL only the header is read.  The degree file is
+ * int32 int_size, uint32 n, uint32 m, int32 degree[n]; the adjacency file is
+ * int32 dst[m].  Returns 0, -6 (cannot open) or -7 (short file). */
+int oracle_read_graph(const char *dir, uint32_t *n_out, uint32_t *m_out, uint32_t *off, int32_t *dst) {
+  char path[4096];
+  snprintf(path, sizeof(path), "%s/b_degree.bin", dir);
+  FILE *f = fopen(path, "rb");
+  if (!f) return -6;
+  int32_t int_size;
+  uint32_t n, m;
+  if (fread(&int_size, 4, 1, f) != 1 || fread(&n, 4, 1, f) != 1 || fread(&m, 4, 1, f) != 1) { fclose(f); return -7; }
+  *n_out = n; *m_out = m;
+  if (!off) { fclose(f); return 0; }
+  off[0] = 0;
+  for (uint32_t i = 0; i < n; i++) {
+    int32_t d;
+    if (fread(&d, 4, 1, f) != 1) { fclose(f); return -7; }
+    off[i + 1] = off[i] + (uint32_t)d;
+  }
+  fclose(f);
+  snprintf(path, sizeof(path), "%s/b_adj.bin", dir);
+  f = fopen(path, "rb");
+  if (!f) return -6;
+  size_t got = fread(dst, 4, m, f);
+  fclose(f);
+  return got == m ? 0 : -7;
+}
+
+/* The whole reference pipeline on one graph: count, similarity, cores, clusters,
+ * hubs, pairs and (when dir != NULL) the result file.  sim/label/cluster are
+ * caller buffers of m/n/n entries; returns the number of non-core pairs or a
+ * negative status. */
+int64_t oracle_scan(uint32_t n, const uint32_t *off, const int32_t *dst, double eps, int mu, int nthreads,
+                    int32_t *cnn, uint8_t *sim, int32_t *core_count, int32_t *label, int32_t *cluster,
+                    const char *dir) {
+  int rc = oracle_cn_count(n, off, dst, cnn, nthreads);
+  if (rc) return rc;
+  oracle_similarity(n, off, dst, cnn, eps, mu, sim, core_count, label);
+  oracle_cluster(n, off, dst, sim, label, cluster);
+  int64_t k = oracle_noncore_pairs(n, off, dst, sim, label, cluster, NULL);
+  int32_t *pairs = (int32_t *)malloc(sizeof(int32_t) * 2 * (size_t)(k ? k : 1));
+  int64_t np = oracle_noncore_pairs(n, off, dst, sim, label, cluster, pairs);
+  if (dir) rc = oracle_write_result(dir, eps, mu, n, label, cluster, pairs, np);
+  free(pairs);
+  return rc ? rc : np;
+}
+
+/* The reference's similarity expression for one (cnn, du, dv) triple, evaluated
+ * in this host's long double exactly as CheckCoreCompSimCore does; fills
+ * out[i] for k triples (used to check the exact-integer predicate). */
+void oracle_sim_batch(int64_t k, const uint32_t *cnn, const uint32_t *du, const uint32_t *dv, double eps,
+                      uint8_t *out) {
+  for (int64_t i = 0; i < k; i++) {
+    long double a = du[i], b = dv[i];
+    double sim_value = (double)((long double)cnn[i] / sqrtl(a * b));
+    out[i] = sim_value >= eps;
+  }
+}
+
+/* The CheckCoreBitmap work of a subset of owner vertices (a bounded sample of a
+ * full count, used to time the CPU baseline): for each listed u, the owned
+ * entries of u get cnn[e] = 2 + count and their reverse entries the same value.
+ * Returns the number of owned edges processed (each fills two CSR entries). */
+int64_t oracle_cn_count_owners(uint32_t n, const uint32_t *off, const int32_t *dst, const uint32_t *owners,
+                               int64_t k, int nthreads, int32_t *cnn) {
+  int64_t done = 0;
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel num_threads(nthreads) reduction(+ : done)
+#endif
+  {
+    uint8_t *bits = (uint8_t *)calloc(n ? n : 1, 1);
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 16)
+#endif
+    for (int64_t i = 0; i < k; i++) {
+      uint32_t u = owners[i];
+      uint32_t du = off[u + 1] - off[u];
+      for (uint32_t e = off[u]; e < off[u + 1]; e++) bits[dst[e]] = 1;
+      for (uint32_t e = off[u]; e < off[u + 1]; e++) {
+        uint32_t v = (uint32_t)dst[e];
+        uint32_t dv = off[v + 1] - off[v];
+        if (!(du > dv || (du == dv && u < v))) continue;
+        int32_t c = 0;
+        for (uint32_t f = off[v]; f < off[v + 1]; f++) c += bits[dst[f]];
+        cnn[e] = 2 + c;
+        uint32_t r = orc_binary_search(dst, off[v], off[v + 1], (int32_t)u);
+        if (r != UINT32_MAX) cnn[r] = cnn[e];
+        done++;
+      }
+      for (uint32_t e = off[u]; e < off[u + 1]; e++) bits[dst[e]] = 0;
+    }
+    free(bits);
+  }
+  return done;
+}

@@ -1,0 +1,157 @@
+"""GPU parity: the sm_103a kernels behind the C ABI against the reference's own
+outputs (golden fixtures) and against the oracle on larger seeded graphs.
+Counts, similarity bits, labels, clusters and result files must match bit for
+bit, for every counting policy and for bitmap windows small enough to force
+many windows."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import golden_cases, has_gpu, load_golden
+
+pytestmark = pytest.mark.gpu
+
+if has_gpu():
+    from acctricnt_gb300 import accx
+    from oracle import oracle
+
+POLICIES = ["heuristic", "merge", "gallop", "bitmap"]
+
+
+def _table(seed):
+    rng = np.random.default_rng(seed)
+    return rng.integers(0, 3, size=(24, 24)).astype(np.uint8)
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_counts_match_reference_all_policies(name):
+    g = load_golden(name)
+    G = accx.Graph.from_csr(g["off"], g["dst"])
+    for pol in POLICIES:
+        cnt = G.count(policy=pol, bias=2)
+        assert np.array_equal(cnt, g["cnn"]), pol
+    cnt = G.count(policy="table", table=_table(1), bias=2)
+    assert np.array_equal(cnt, g["cnn"])
+    # tiny bitmap windows: 1 KiB = 8192 ids per window, many windows per owner
+    cnt = G.count(policy="bitmap", bias=2, window_kb=1, block_warps=4)
+    assert np.array_equal(cnt, g["cnn"])
+    raw = G.count(policy="heuristic", bias=0)
+    assert np.array_equal(raw + 2, g["cnn"])
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_scan_matches_reference(name, tmp_path):
+    g = load_golden(name)
+    G = accx.Graph.from_csr(g["off"], g["dst"])
+    G.count(policy="heuristic", bias=0, out=None)
+    r = G.scan(float(g["eps"]), int(g["mu"]))
+    assert np.array_equal(r["sim"], g["sim"])
+    assert np.array_equal(r["label"], g["label"])
+    assert np.array_equal(r["cluster"], g["cluster"])
+    s = r["summary"]
+    assert s["cores"] == int((g["label"] == 1).sum())
+    assert s["hubs"] == int((g["label"] == 2).sum())
+    assert s["outliers"] == int((g["label"] == 0).sum())
+    G.write_result(str(tmp_path), float(g["eps"]), int(g["mu"]))
+    with open(os.path.join(str(tmp_path), str(g["result_name"])), "rb") as f:
+        assert f.read() == g["result"].tobytes()
+
+
+@pytest.mark.parametrize("params", [
+    ("rmat", 12, 16, 1), ("rmat", 14, 8, 2), ("er", 5000, 20, 3), ("cl", 20000, 16, 4)])
+def test_device_generator_matches_host(params):
+    kind = params[0]
+    if kind == "rmat":
+        p = accx.rmat_params(params[1], params[2], seed=params[3])
+    elif kind == "er":
+        p = accx.er_params(params[1], params[2], seed=params[3])
+    else:
+        p = accx.chung_lu_params(params[1], params[2], 2.1, 3000, seed=params[3])
+    off_h, dst_h = accx.generate_host(p)
+    G = accx.Graph.generate(p)
+    off_d, dst_d = G.download()
+    assert np.array_equal(off_h, off_d) and np.array_equal(dst_h, dst_d)
+
+
+@pytest.mark.parametrize("eps,mu", [(0.2, 5), (0.5, 5), (0.8, 5)])
+def test_rmat16_full_parity_with_oracle(eps, mu, tmp_path):
+    """R-MAT scale 16, edge factor 16 (65,536 vertices): the plain CPU config."""
+    p = accx.rmat_params(16, 16, seed=1)
+    G = accx.Graph.generate(p)
+    off, dst = G.download()
+    ref = oracle.scan(off, dst, eps, mu, nthreads=8, out_dir=str(tmp_path))
+    for pol in POLICIES:
+        assert np.array_equal(G.count(policy=pol, bias=2), ref["cnn"]), pol
+    r = G.scan(eps, mu)
+    assert np.array_equal(r["sim"], ref["sim"])
+    assert np.array_equal(r["label"], ref["label"])
+    assert np.array_equal(r["cluster"], ref["cluster"])
+    assert np.array_equal(G.pairs(), ref["pairs"])
+    name = "scanxp-result-%s-%d.txt" % (oracle.eps_string(eps), mu)
+    os.rename(os.path.join(str(tmp_path), name), os.path.join(str(tmp_path), "oracle.txt"))
+    G.write_result(str(tmp_path), eps, mu)
+    with open(os.path.join(str(tmp_path), name), "rb") as a, open(os.path.join(str(tmp_path), "oracle.txt"), "rb") as b:
+        assert a.read() == b.read()
+
+
+def test_chung_lu_skew_parity_with_oracle():
+    """Power-law graph with a heavy head: every policy equals the oracle."""
+    p = accx.chung_lu_params(200000, 24, 2.1, 20000, seed=7)
+    G = accx.Graph.generate(p)
+    off, dst = G.download()
+    ref = oracle.cn_count(off, dst, nthreads=8)
+    for pol in POLICIES:
+        assert np.array_equal(G.count(policy=pol, bias=2), ref), pol
+
+
+def test_large_rmat_policies_agree_and_are_symmetric():
+    """Size-independent properties at R-MAT scale 20: all policies agree, the
+    count array is symmetric (cnt[e] == cnt[reverse(e)]), and sampled entries
+    equal an independent numpy set intersection."""
+    G = accx.Graph.generate(accx.rmat_params(20, 16, seed=1))
+    off, dst = G.download()
+    base = G.count(policy="heuristic")
+    for pol in ["merge", "bitmap", "gallop"]:
+        assert np.array_equal(G.count(policy=pol), base), pol
+    n = len(off) - 1
+    src = np.repeat(np.arange(n, dtype=np.int64), np.diff(off).astype(np.int64))
+    key = src * n + dst
+    rkey = dst.astype(np.int64) * n + src
+    order = np.argsort(key)
+    pos = order[np.searchsorted(key[order], rkey)]
+    assert np.array_equal(base[pos], base)
+    rng = np.random.default_rng(0)
+    for e in rng.integers(0, len(dst), 2000):
+        u, v = src[e], dst[e]
+        a = dst[off[u]:off[u + 1]]
+        b = dst[off[v]:off[v + 1]]
+        assert base[e] == len(np.intersect1d(a, b, assume_unique=True))
+
+
+@pytest.mark.parametrize("bad", ["self_loop", "unsorted", "asymmetric", "range"])
+def test_invalid_graphs_rejected(bad):
+    off = np.array([0, 2, 4, 6], np.uint32)
+    dst = np.array([1, 2, 0, 2, 0, 1], np.int32)
+    code = {"self_loop": accx.ERR_SELF_LOOP, "unsorted": accx.ERR_UNSORTED, "asymmetric": accx.ERR_ASYMMETRIC,
+            "range": accx.ERR_RANGE}[bad]
+    if bad == "self_loop":
+        dst = np.array([0, 2, 0, 2, 0, 1], np.int32)
+    elif bad == "unsorted":
+        dst = np.array([2, 1, 0, 2, 0, 1], np.int32)
+    elif bad == "asymmetric":
+        off = np.array([0, 2, 3, 5], np.uint32)
+        dst = np.array([1, 2, 0, 0, 1], np.int32)
+    else:
+        dst = np.array([1, 9, 0, 2, 0, 1], np.int32)
+    with pytest.raises(accx.AccxError) as ei:
+        accx.Graph.from_csr(off, dst)
+    assert ei.value.status == code
+
+
+def test_query_before_count_is_not_ready():
+    off, dst = accx.generate_host(accx.rmat_params(8, 8))
+    G = accx.Graph.from_csr(off, dst)
+    with pytest.raises(accx.AccxError) as ei:
+        G.scan(0.5, 2)
+    assert ei.value.status == accx.ERR_NOT_READY

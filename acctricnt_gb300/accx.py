@@ -41,7 +41,7 @@ class GenParams(C.Structure):
 
 class CountOpts(C.Structure):
     _fields_ = [("policy", C.c_int), ("table", C.POINTER(C.c_uint8)), ("bias", C.c_int32),
-                ("block_warps", C.c_int), ("bitmap_window_kb", C.c_int), ("timing", C.c_int)]
+                ("block_warps", C.c_int), ("bitmap_window_kb", C.c_int), ("timing", C.c_int), ("sparse_table_kb", C.c_int)]
 
 
 class ScanSummary(C.Structure):
@@ -67,6 +67,8 @@ def _load():
         "accx_graph_download": (C.c_int, [P, P, P, P]),
         "accx_graph_device_ptrs": (C.c_int, [P, C.POINTER(P), C.POINTER(P), C.POINTER(P)]),
         "accx_graph_generate": (C.c_int, [C.POINTER(GenParams), P, C.POINTER(P)]),
+        "accx_graph_relabel": (C.c_int, [P, P]),
+        "accx_graph_is_relabeled": (C.c_int, [P]),
         "accx_generate_host": (C.c_int, [C.POINTER(GenParams), C.POINTER(C.c_uint32), C.POINTER(C.c_uint64), P, P]),
         "accx_write_graph_dir": (C.c_int, [C.c_char_p, P, P, C.c_uint32, C.c_uint64]),
         "accx_cn_count": (C.c_int, [P, C.POINTER(CountOpts), P, P]),
@@ -209,6 +211,14 @@ class Graph:
         _check(lib.accx_graph_generate(C.byref(params), _stream_ptr(stream), C.byref(h)), "graph_generate")
         return cls(h)
 
+    def relabel(self, stream=None):
+        """Degree-descending relabeled copy for counting (results unchanged)."""
+        _check(lib.accx_graph_relabel(self._h, _stream_ptr(stream)), "graph_relabel")
+
+    @property
+    def relabeled(self):
+        return bool(lib.accx_graph_is_relabeled(self._h))
+
     def free(self):
         if self._h:
             lib.accx_graph_free(self._h)
@@ -232,7 +242,7 @@ class Graph:
         return o.value, d.value, c.value
 
     @staticmethod
-    def _opts(policy, table, bias, block_warps, window_kb, timing=False):
+    def _opts(policy, table, bias, block_warps, window_kb, timing=False, sparse_kb=0):
         pol = POLICIES[policy] if isinstance(policy, str) else int(policy)
         tab = None
         keep = None
@@ -242,13 +252,13 @@ class Graph:
             tab = keep.ctypes.data_as(C.POINTER(C.c_uint8))
             if pol == POLICY_HEURISTIC and isinstance(policy, str) and policy == "heuristic":
                 pass
-        return CountOpts(pol, tab, int(bias), int(block_warps), int(window_kb), 1 if timing else 0), keep
+        return CountOpts(pol, tab, int(bias), int(block_warps), int(window_kb), 1 if timing else 0, int(sparse_kb)), keep
 
     def count(self, policy="heuristic", table=None, bias=0, out="host", block_warps=0, window_kb=0, stream=None,
-              timing=False):
+              timing=False, sparse_kb=0):
         """All-edge CN counts.  out="host" returns an int32 numpy array; out=None
         leaves them resident; out=<int device pointer> copies there."""
-        opts, keep = self._opts(policy, table, bias, block_warps, window_kb, timing)
+        opts, keep = self._opts(policy, table, bias, block_warps, window_kb, timing, sparse_kb)
         if out == "host":
             res = np.zeros(max(self.m, 1), np.int32)
             _check(lib.accx_cn_count(self._h, C.byref(opts), _ptr(res), _stream_ptr(stream)), "cn_count")

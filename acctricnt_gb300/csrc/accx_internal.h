@@ -12,11 +12,6 @@
 // a list's last window never leave the allocation.
 #define ACCX_DST_PAD 64
 
-// Bitmap-kernel work item: owner u, its CSR entry range [e0, e1).
-struct accx_bitmap_item {
-  uint32_t u, e0, e1, pad;
-};
-
 struct accx_graph {
   int device = 0;
   uint32_t n = 0;
@@ -24,13 +19,22 @@ struct accx_graph {
   uint32_t *d_off = nullptr;  // n+1
   int32_t *d_dst = nullptr;   // m + ACCX_DST_PAD
   int32_t *d_cnt = nullptr;   // m
+  // degree-descending relabel (accx_graph_relabel): counting runs on these
+  uint32_t *d_roff = nullptr;   // n+1
+  int32_t *d_rdst = nullptr;    // m + ACCX_DST_PAD
+  uint32_t *d_rmap = nullptr;   // m: original entry -> relabeled entry
+  int32_t *d_rcnt = nullptr;    // m: counts in relabeled order
+  uint32_t *d_oldid = nullptr;  // n: new id -> original id
+  uint32_t *d_newid = nullptr;  // n: original id -> new id
   int32_t cnt_bias = 0;
   bool cnt_valid = false;
 
   // counting scratch
   uint2 *d_edge_list = nullptr;  // m/2+1 owned entries: merge items from the front, gallop from the back
-  accx_bitmap_item *d_items = nullptr;
-  uint64_t items_cap = 0;
+  unsigned long long *d_icnt = nullptr;    // n+1 bitmap items per owner
+  unsigned long long *d_prefix = nullptr;  // n+1 exclusive prefix of d_icnt
+  void *d_scan_tmp = nullptr;
+  size_t scan_tmp_bytes = 0;
   unsigned long long *d_counters = nullptr;  // [0] merge, [1] gallop, [2] bitmap items, [3..5] work per kind
   uint64_t stats_edges[ACCX_NUM_KINDS] = {0, 0, 0};
   uint64_t stats_work[ACCX_NUM_KINDS] = {0, 0, 0};
@@ -93,5 +97,8 @@ void accx_model_release(accx_graph *g);
 int accx_model_table(accx_graph *g, uint8_t *table);
 
 // Exclusive/inclusive helpers implemented in gen.cu.
+// Relabeled counts -> the handle's entry order (relabel.cu).
+int accx_relabel_gather(accx_graph *g, cudaStream_t s);
+
 int accx_build_csr_from_keys(accx_graph *g, unsigned long long *d_keys, uint64_t nkeys, uint32_t n,
                              cudaStream_t s);

@@ -21,6 +21,8 @@
 // fixed sequence of launches on one stream (capturable in a CUDA graph).
 #include <string.h>
 
+#include <cub/cub.cuh>
+
 #include "accx_internal.h"
 #include "devutil.cuh"
 
@@ -35,7 +37,7 @@
 
 #define MERGE_WIN 128        // int32 per list window (32 lanes x uint4)
 #define MERGE_WARPS 8        // warps per merge/gallop CTA
-#define ITEM_TARGET_DEFAULT (1u << 17)  // probe elements per bitmap work item
+#define ITEM_TARGET_DEFAULT (1u << 20)  // probe elements per bitmap work item
 
 // Kind of an owned edge; du = owner degree >= dv.
 __device__ __forceinline__ int accx_edge_kind(int policy, const uint8_t *table, uint32_t du, uint32_t dv) {
@@ -109,33 +111,6 @@ __global__ void __launch_bounds__(TILE) k_classify(const uint32_t *__restrict__ 
       unsigned peers = __match_any_sync(mask, u);
       unsigned sw = __reduce_add_sync(peers, dv);
       if (lane == __ffs(peers) - 1) atomicAdd(&work_u[u], (unsigned long long)sw + 1ull);
-    }
-  }
-}
-
-// Bitmap work items: split each bitmap owner's entry range into chunks of about
-// ITEM_TARGET probe elements (at least 64 entries per chunk).
-__global__ void k_make_items(const uint32_t *__restrict__ off, uint32_t n, unsigned long long *__restrict__ work_u,
-                             accx_bitmap_item *__restrict__ items, unsigned long long item_cap, uint32_t target,
-                             unsigned long long *__restrict__ ctr) {
-  for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
-    unsigned long long w = work_u[u];
-    if (!w) continue;
-    work_u[u] = 0;
-    uint32_t b = off[u], e = off[u + 1], d = e - b;
-    unsigned long long k = (w + d + target - 1) / target;
-    unsigned long long kmax = (d + 63) / 64;
-    if (k > kmax) k = kmax;
-    if (k < 1) k = 1;
-    unsigned long long p = atomicAdd(&ctr[C_ITEMS], k);
-    atomicAdd(&ctr[C_OWNER + ACCX_KIND_BITMAP], (unsigned long long)d * k);
-    for (unsigned long long c = 0; c < k && p + c < item_cap; c++) {
-      accx_bitmap_item it;
-      it.u = u;
-      it.e0 = b + (uint32_t)((unsigned long long)d * c / k);
-      it.e1 = b + (uint32_t)((unsigned long long)d * (c + 1) / k);
-      it.pad = 0;
-      items[p + c] = it;
     }
   }
 }
@@ -274,79 +249,341 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32) k_gallop(const uint32_t *__r
 }
 
 // ---------------------------------------------------------------------------
-// Per-owner shared-memory bitmap.
-//
-// A CTA takes a work item (owner u, a slice [e0,e1) of its entries).  The id
-// space is cut into windows of WB ids (WB = 8 x the bitmap bytes); for every
-// window that holds part of N(u) the CTA sets those bits in shared memory, then
-// each warp takes an owned bitmap-kind entry (u,v), finds where N(v) enters the
-// window (binary search), streams N(v) 32 ids at a time, tests the bits and
-// counts hits with ballot/popc, adds the window's count to cnt[e], and the CTA
-// clears the bits it set.  The reference keeps one n-bit bitmap per resident
-// block in global memory and claims it with a CAS spin on per-SM slots
-// (scan_xp_multi_gpu_multi_pass_common.cu:308-407); here nothing is shared
-// between CTAs and nothing spins.
-__global__ void k_bitmap(const uint32_t *__restrict__ off, const int32_t *__restrict__ dst, int policy,
-                         const uint8_t *__restrict__ table, const accx_bitmap_item *__restrict__ items,
-                         unsigned long long item_cap, const unsigned long long *__restrict__ ctr,
-                         uint32_t win_words, int32_t *__restrict__ cnt) {
-  extern __shared__ __align__(16) uint32_t bm[];
+// Bitmap work items.  A bitmap owner u (an owner with at least one bitmap-kind
+// edge) stages N(u) in shared memory as two parts: ids below W in a dense
+// bitmap (after the degree-descending relabel these are the highest-degree
+// vertices, where most probes land), ids from W up as (word index -> 32-bit
+// word) pairs in an open-addressing table.  If the upper part has more ids than
+// half the table's slots it is cut into chunks; the owner then becomes
+// nchunks x nsplit virtual items (chunk c, split s probes the owned entries in
+// the s-th slice of N(u)).  Only per-owner item counts are stored; a CTA maps an
+// item index to its owner by a warp-parallel search over their prefix.
+__device__ __forceinline__ void accx_item_shape(uint32_t du, uint32_t nsp, unsigned long long work, uint32_t chs,
+                                                uint32_t target, uint32_t *nchunks, uint32_t *nsplit) {
+  uint32_t nc = (nsp + chs - 1) / chs;
+  if (nc < 1) nc = 1;
+  unsigned long long per = (unsigned long long)nc * target;
+  unsigned long long ns = (work + per - 1) / per;
+  unsigned long long nsmax = du / 32 > 1 ? du / 32 : 1;
+  if (ns > nsmax) ns = nsmax;
+  if (ns < 1) ns = 1;
+  *nchunks = nc;
+  *nsplit = (uint32_t)ns;
+}
+
+__global__ void k_item_counts(const uint32_t *__restrict__ off, const int32_t *__restrict__ dst, uint32_t n,
+                              const unsigned long long *__restrict__ work_u, uint32_t W, uint32_t chs,
+                              uint32_t target, unsigned long long *__restrict__ icnt,
+                              unsigned long long *__restrict__ ctr) {
+  for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u <= n; u += gridDim.x * blockDim.x) {
+    unsigned long long c = 0;
+    if (u < n) {
+      unsigned long long w = work_u[u];
+      if (w) {
+        uint32_t ub = off[u], ue = off[u + 1];
+        uint32_t us = accx_lower_bound(dst, ub, ue, (int32_t)min(W, 0x7fffffffu));
+        uint32_t nc, ns;
+        accx_item_shape(ue - ub, ue - us, w, chs, target, &nc, &ns);
+        c = (unsigned long long)nc * ns;
+        atomicAdd(&ctr[C_OWNER + ACCX_KIND_BITMAP], (unsigned long long)(ue - ub) * ns);
+      }
+    }
+    icnt[u] = c;
+  }
+}
+
+__device__ __forceinline__ uint32_t accx_slot_hash(uint32_t word, uint32_t S) {
+  return __umulhi(word * 0x9E3779B1u, S);
+}
+
+__device__ __forceinline__ void accx_sparse_insert(uint2 *slots, uint32_t S, uint32_t x) {
+  const uint32_t key = (x >> 5) + 1u;
+  uint32_t h = accx_slot_hash(x >> 5, S);
+  for (uint32_t it = 0; it < S; it++) {
+    uint32_t prev = atomicCAS(&slots[h].x, 0u, key);
+    if (prev == 0u || prev == key) {
+      atomicOr(&slots[h].y, 1u << (x & 31));
+      return;
+    }
+    h = (h + 1 == S) ? 0 : h + 1;
+  }
+}
+
+__device__ __forceinline__ uint32_t accx_sparse_find(const uint2 *slots, uint32_t S, uint32_t x, bool *hit) {
+  const uint32_t key = (x >> 5) + 1u;
+  uint32_t h = accx_slot_hash(x >> 5, S);
+  for (uint32_t it = 0; it < S; it++) {
+    uint2 s = slots[h];
+    if (s.x == key) {
+      *hit = (s.y >> (x & 31)) & 1u;
+      return h;
+    }
+    if (s.x == 0u) break;
+    h = (h + 1 == S) ? 0 : h + 1;
+  }
+  *hit = false;
+  return 0xffffffffu;
+}
+
+struct accx_bm_view {
+  const uint32_t *words;
+  const uint2 *slots;
+  uint32_t W, S;
+  bool has_sparse;
+};
+
+__device__ __forceinline__ uint32_t accx_bm_test(const accx_bm_view &b, uint32_t x) {
+  if (x < b.W) return (b.words[x >> 5] >> (x & 31)) & 1u;
+  if (!b.has_sparse) return 0u;
+  bool hit;
+  accx_sparse_find(b.slots, b.S, x, &hit);
+  return hit ? 1u : 0u;
+}
+
+#define PROBE_UNROLL 4
+#define LONG_SEG 64
+
+// One CTA per virtual item (grid-stride).  Per round of up to blockDim owned
+// entries, each thread takes one entry (u,v) and the part of N(v) to probe.
+// Long parts (>= LONG_SEG ids) are pulled by whole warps and streamed with
+// 16-byte loads; short parts are concatenated (CTA prefix sum) and streamed 32
+// ids per warp step, a lane finding its entry from a ballot-built boundary mask.
+// Hits are counted per entry (registers for long parts, shared counters for
+// short ones).
+__global__ void __launch_bounds__(1024, 1) k_bitmap(const uint32_t *__restrict__ off, const int32_t *__restrict__ dst,
+                                                    uint32_t n, int policy, const uint8_t *__restrict__ table,
+                                                    const unsigned long long *__restrict__ work_u,
+                                                    const unsigned long long *__restrict__ prefix, uint32_t W,
+                                                    uint32_t S, uint32_t target, int32_t *__restrict__ cnt) {
+  extern __shared__ __align__(16) uint32_t smem[];
+  uint32_t *words = smem;                                   // W/32 dense words
+  uint2 *slots = reinterpret_cast<uint2 *>(smem + W / 32);  // S sparse slots
   __shared__ uint8_t s_table[ACCX_NB * ACCX_NB];
-  __shared__ uint32_t s_wend;
+  __shared__ uint32_t s_u, s_us, s_tot, s_nseg, s_nlong, s_lnext;
+  __shared__ uint32_t s_wsum[32], s_wcnt[32], s_wlong[32];
+  __shared__ uint32_t s_pre[1025], s_beg[1024], s_ent[1024], s_hit[1024];
+  __shared__ uint32_t s_lbeg[1024], s_llen[1024], s_lent[1024];
   const int tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
-  const uint32_t WB = win_words * 32u;
+  const uint32_t CHS = S / 2;
+  const uint32_t nwords = W / 32;
   for (int i = tid; i < ACCX_NB * ACCX_NB; i += nt) s_table[i] = table ? table[i] : 0;
-  for (uint32_t i = tid; i < win_words; i += nt) bm[i] = 0;
+  for (uint32_t i = tid; i < nwords; i += nt) words[i] = 0;
+  for (uint32_t i = tid; i < S; i += nt) slots[i] = make_uint2(0u, 0u);
+  const unsigned long long total = prefix[n];
   __syncthreads();
-  unsigned long long total = ctr[C_ITEMS];
-  if (total > item_cap) total = item_cap;
   for (unsigned long long it = blockIdx.x; it < total; it += gridDim.x) {
-    accx_bitmap_item item = items[it];
-    const uint32_t u = item.u;
-    const uint32_t ub = off[u], ue = off[u + 1], du = ue - ub;
-    uint32_t pos = ub;
-    while (pos < ue) {
-      const uint32_t wlo = ((uint32_t)__ldg(dst + pos) / WB) * WB;
-      const uint32_t whi = wlo + WB;  // may wrap only past 2^32 ids, impossible for int32 ids
-      if (tid == 0) s_wend = accx_lower_bound(dst, pos, ue, (int32_t)min(whi, 0x7fffffffu));
-      __syncthreads();
-      const uint32_t wend = (whi > 0x7fffffffu) ? ue : s_wend;
-      for (uint32_t i = pos + tid; i < wend; i += nt) {
-        uint32_t x = (uint32_t)__ldg(dst + i) - wlo;
-        if (x < WB) atomicOr(&bm[x >> 5], 1u << (x & 31));  // always true for sorted rows
+    if (warp == 0) {
+      // largest u in [0, n) with prefix[u] <= it (that owner has >= 1 item)
+      uint32_t lo = 0, hi = n;
+      while (hi - lo > 1) {
+        uint32_t step = (hi - lo + 31) / 32;
+        uint32_t p = lo + (uint32_t)lane * step;
+        bool ok = p < hi && prefix[p] <= it;
+        unsigned b = __ballot_sync(ACCX_FULL_MASK, ok);
+        lo = lo + (31 - __clz(b)) * step;
+        uint32_t nh = lo + step;
+        hi = nh < hi ? nh : hi;
       }
-      __syncthreads();
-      for (uint32_t k = item.e0 + warp; k < item.e1; k += nwarps) {
+      if (lane == 0) {
+        s_u = lo;
+        s_us = accx_lower_bound(dst, off[lo], off[lo + 1], (int32_t)min(W, 0x7fffffffu));
+      }
+    }
+    __syncthreads();
+    const uint32_t u = s_u, us = s_us;
+    const uint32_t ub = off[u], ue = off[u + 1], du = ue - ub;
+    uint32_t nchunks, nsplit;
+    accx_item_shape(du, ue - us, work_u[u], CHS, target, &nchunks, &nsplit);
+    const uint32_t j = (uint32_t)(it - prefix[u]);
+    const uint32_t c = j / nsplit, sp = j % nsplit;
+    const uint32_t ca = min(ue, us + c * CHS), cb = min(ue, ca + CHS);
+    const uint32_t pa = ub + (uint32_t)((unsigned long long)du * sp / nsplit);
+    const uint32_t pb = ub + (uint32_t)((unsigned long long)du * (sp + 1) / nsplit);
+    const bool windowed = nchunks > 1;
+    const bool dense_part = (c == 0) && us > ub;
+    accx_bm_view bv{words, slots, W, S, cb > ca};
+    const int32_t u_lo = __ldg(dst + ub), u_hi = __ldg(dst + ue - 1);
+    const int32_t c_lo = cb > ca ? __ldg(dst + ca) : 0, c_hi = cb > ca ? __ldg(dst + cb - 1) : 0;
+    // stage
+    if (dense_part)
+      for (uint32_t i = ub + tid; i < us; i += nt) {
+        uint32_t x = (uint32_t)__ldg(dst + i);
+        if (x < W) atomicOr(&words[x >> 5], 1u << (x & 31));
+      }
+    for (uint32_t i = ca + tid; i < cb; i += nt) accx_sparse_insert(slots, S, (uint32_t)__ldg(dst + i));
+    __syncthreads();
+    // probe, one round of up to nt owned entries at a time
+    for (uint32_t r0 = pa; r0 < pb; r0 += (uint32_t)nt) {
+      const uint32_t k = r0 + (uint32_t)tid;
+      uint32_t sst = 0, len = 0;
+      if (k < pb) {
         const uint32_t v = (uint32_t)__ldg(dst + k);
         const uint32_t vb = __ldg(off + v), ve = __ldg(off + v + 1), dv = ve - vb;
-        if (dv == 0 || !accx_owns(u, du, v, dv) || accx_edge_kind(policy, s_table, du, dv) != ACCX_KIND_BITMAP)
-          continue;
-        if (__ldg(dst + ve - 1) < (int32_t)wlo || __ldg(dst + vb) >= (int32_t)min(whi, 0x7fffffffu)) continue;
-        uint32_t s = accx_lower_bound(dst, vb, ve, (int32_t)wlo);
-        uint32_t c = 0;
-        for (uint32_t j0 = s; j0 < ve; j0 += 32) {
-          uint32_t j = j0 + (uint32_t)lane;
-          uint32_t x = (j < ve) ? (uint32_t)__ldg(dst + j) : 0xffffffffu;
-          bool inwin = x < whi && x >= wlo;
-          bool hit = inwin && ((bm[(x - wlo) >> 5] >> ((x - wlo) & 31)) & 1u);
-          c += __popc(__ballot_sync(ACCX_FULL_MASK, hit));
-          if (__ballot_sync(ACCX_FULL_MASK, !inwin)) break;
-        }
-        if (lane == 0 && c) cnt[k] += (int32_t)c;
-      }
-      __syncthreads();
-      if (wend - pos > win_words / 8) {
-        for (uint32_t i = tid; i < win_words; i += nt) bm[i] = 0;
-      } else {
-        for (uint32_t i = pos + tid; i < wend; i += nt) {
-          uint32_t x = (uint32_t)__ldg(dst + i) - wlo;
-          if (x < WB) bm[x >> 5] = 0;
+        if (dv > 0 && accx_owns(u, du, v, dv) &&
+            accx_edge_kind(policy, s_table, du, dv) == ACCX_KIND_BITMAP) {
+          uint32_t t = ve;
+          sst = vb;
+          if (!windowed) {
+            if (__ldg(dst + ve - 1) < u_lo || __ldg(dst + vb) > u_hi) t = sst;  // disjoint id spans
+          } else {
+            if (c > 0) sst = accx_lower_bound(dst, vb, ve, c_lo);
+            t = accx_lower_bound(dst, sst, ve, c_hi + 1);
+          }
+          len = t - sst;  // an empty part leaves the zeroed count in place
         }
       }
+      // compact: short parts (prefix-summed) and long parts (a work list)
+      const bool is_short = len > 0 && len < LONG_SEG, is_long = len >= LONG_SEG;
+      const unsigned bs = __ballot_sync(ACCX_FULL_MASK, is_short), bl = __ballot_sync(ACCX_FULL_MASK, is_long);
+      const uint32_t slen = is_short ? len : 0u;
+      uint32_t incl = slen;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        uint32_t y = __shfl_up_sync(ACCX_FULL_MASK, incl, d);
+        if (lane >= d) incl += y;
+      }
+      if (lane == 31) {
+        s_wsum[warp] = incl;
+        s_wcnt[warp] = __popc(bs);
+        s_wlong[warp] = __popc(bl);
+      }
       __syncthreads();
-      pos = wend;
+      if (warp == 0) {
+        uint32_t ws = lane < nwarps ? s_wsum[lane] : 0u, wc = lane < nwarps ? s_wcnt[lane] : 0u;
+        uint32_t wl = lane < nwarps ? s_wlong[lane] : 0u;
+        uint32_t is = ws, ic = wc, il = wl;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          uint32_t y = __shfl_up_sync(ACCX_FULL_MASK, is, d), z = __shfl_up_sync(ACCX_FULL_MASK, ic, d);
+          uint32_t q = __shfl_up_sync(ACCX_FULL_MASK, il, d);
+          if (lane >= d) { is += y; ic += z; il += q; }
+        }
+        if (lane < nwarps) { s_wsum[lane] = is - ws; s_wcnt[lane] = ic - wc; s_wlong[lane] = il - wl; }
+        if (lane == 31) { s_tot = is; s_nseg = ic; s_nlong = il; s_lnext = 0; }
+      }
+      __syncthreads();
+      if (is_short) {
+        const uint32_t idx = s_wcnt[warp] + __popc(bs & ((1u << lane) - 1u));
+        s_pre[idx] = s_wsum[warp] + incl - len;
+        s_beg[idx] = sst;
+        s_ent[idx] = k;
+        s_hit[idx] = 0;
+      }
+      if (is_long) {
+        const uint32_t idx = s_wlong[warp] + __popc(bl & ((1u << lane) - 1u));
+        s_lbeg[idx] = sst;
+        s_llen[idx] = len;
+        s_lent[idx] = k;
+      }
+      __syncthreads();
+      const uint32_t tot = s_tot, nseg = s_nseg, nlong = s_nlong;
+      if (tid == 0) s_pre[nseg] = tot;
+      __syncthreads();
+      // short parts: each warp takes 32*PROBE_UNROLL consecutive ids of the concatenation
+      for (uint32_t c0 = (uint32_t)warp * 32u * PROBE_UNROLL; c0 < tot; c0 += (uint32_t)nwarps * 32u * PROBE_UNROLL) {
+        uint32_t lo = 0, hi = nseg;
+        while (hi - lo > 1) {
+          uint32_t step = (hi - lo + 31) / 32;
+          uint32_t p = lo + (uint32_t)lane * step;
+          unsigned b = __ballot_sync(ACCX_FULL_MASK, p < hi && s_pre[p] <= c0);
+          lo += (31 - __clz(b)) * step;
+          uint32_t nh = lo + step;
+          hi = nh < hi ? nh : hi;
+        }
+        // segb = part holding the sub-chunk's first id; 32 ids meet at most 31
+        // part starts after it, so each lane loads one start, the warp ORs them
+        // into a mask by offset, and a lane's part is segb + (starts at or before it).
+        uint32_t segb = lo;
+        int32_t xs[PROBE_UNROLL];
+        uint32_t sg[PROBE_UNROLL];
+#pragma unroll
+        for (int r = 0; r < PROBE_UNROLL; r++) {
+          const uint32_t i0 = c0 + 32u * r;
+          const uint32_t i = i0 + (uint32_t)lane;
+          const uint32_t kb = segb + 1u + (uint32_t)lane;
+          const uint32_t bnd = kb <= nseg ? s_pre[kb] : 0xffffffffu;
+          const uint32_t o = bnd - i0;  // >= 1: part segb holds i0
+          const unsigned M = __reduce_or_sync(ACCX_FULL_MASK, o < 32u ? (1u << o) : 0u);
+          const uint32_t sj = segb + __popc(M & (lane == 31 ? 0xffffffffu : ((2u << lane) - 1u)));
+          sg[r] = sj;
+          xs[r] = (i < tot) ? __ldg(dst + s_beg[sj] + (i - s_pre[sj])) : -1;
+          segb += __popc(M) + (__ballot_sync(ACCX_FULL_MASK, o == 32u) ? 1u : 0u);
+        }
+#pragma unroll
+        for (int r = 0; r < PROBE_UNROLL; r++)
+          if (xs[r] >= 0 && accx_bm_test(bv, (uint32_t)xs[r])) atomicAdd(&s_hit[sg[r]], 1u);
+      }
+      // long parts: whole warps, 16-byte loads
+      for (;;) {
+        uint32_t q = 0;
+        if (lane == 0) q = atomicAdd(&s_lnext, 1u);
+        q = __shfl_sync(ACCX_FULL_MASK, q, 0);
+        if (q >= nlong) break;
+        const uint32_t a0 = s_lbeg[q], a1 = a0 + s_llen[q];
+        const uint32_t al = min(a1, (a0 + 3u) & ~3u), bl4 = max(al, a1 & ~3u);
+        uint32_t h = 0;
+        if (a0 + (uint32_t)lane < al) h += accx_bm_test(bv, (uint32_t)__ldg(dst + a0 + lane));
+        if (bl4 + (uint32_t)lane < a1) h += accx_bm_test(bv, (uint32_t)__ldg(dst + bl4 + lane));
+        for (uint32_t jj = al + 4u * (uint32_t)lane; jj < bl4; jj += 256u) {
+          const int4 q0 = __ldg(reinterpret_cast<const int4 *>(dst + jj));
+          int4 q1 = make_int4(-1, -1, -1, -1);
+          if (jj + 128u < bl4) q1 = __ldg(reinterpret_cast<const int4 *>(dst + jj + 128u));
+          h += accx_bm_test(bv, (uint32_t)q0.x) + accx_bm_test(bv, (uint32_t)q0.y) +
+               accx_bm_test(bv, (uint32_t)q0.z) + accx_bm_test(bv, (uint32_t)q0.w);
+          if (q1.x >= 0)
+            h += accx_bm_test(bv, (uint32_t)q1.x) + accx_bm_test(bv, (uint32_t)q1.y) +
+                 accx_bm_test(bv, (uint32_t)q1.z) + accx_bm_test(bv, (uint32_t)q1.w);
+        }
+        h = __reduce_add_sync(ACCX_FULL_MASK, h);
+        if (lane == 0) {
+          const uint32_t kk = s_lent[q];
+          if (windowed) {
+            if (h) atomicAdd(&cnt[kk], (int32_t)h);
+          } else {
+            cnt[kk] = (int32_t)h;
+          }
+        }
+      }
+      __syncthreads();
+      for (uint32_t q = tid; q < nseg; q += nt) {
+        const uint32_t h = s_hit[q], kk = s_ent[q];
+        if (windowed) {
+          if (h) atomicAdd(&cnt[kk], (int32_t)h);
+        } else {
+          cnt[kk] = (int32_t)h;
+        }
+      }
+      __syncthreads();
     }
+    // clear what was staged
+    if (dense_part) {
+      if ((us - ub) * 8u > nwords) {
+        for (uint32_t i = tid; i < nwords; i += nt) words[i] = 0;
+      } else {
+        for (uint32_t i = ub + tid; i < us; i += nt) {
+          uint32_t x = (uint32_t)__ldg(dst + i);
+          if (x < W) words[x >> 5] = 0;
+        }
+      }
+    }
+    const uint32_t nel = cb - ca;
+    if (nel && nel <= 4u * (uint32_t)nt) {
+      uint32_t hs[4];
+#pragma unroll
+      for (int r = 0; r < 4; r++) {
+        uint32_t i = ca + tid + (uint32_t)r * nt;
+        bool dummy;
+        hs[r] = i < cb ? accx_sparse_find(slots, S, (uint32_t)__ldg(dst + i), &dummy) : 0xffffffffu;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int r = 0; r < 4; r++)
+        if (hs[r] != 0xffffffffu) slots[hs[r]] = make_uint2(0u, 0u);
+    } else if (nel) {
+      for (uint32_t i = tid; i < S; i += nt) slots[i] = make_uint2(0u, 0u);
+    }
+    __syncthreads();
   }
 }
 
@@ -376,9 +613,13 @@ int accx_ensure_count_scratch(accx_graph *g) {
   const size_t m = g->m, n = g->n;
   if (!g->d_cnt) ACCX_CUDA_TRY(cudaMalloc(&g->d_cnt, sizeof(int32_t) * (m ? m : 1)));
   if (!g->d_edge_list) ACCX_CUDA_TRY(cudaMalloc(&g->d_edge_list, sizeof(uint2) * (m / 2 + 1)));
-  if (!g->d_items) {
-    g->items_cap = n + m / 64 + 1;
-    ACCX_CUDA_TRY(cudaMalloc(&g->d_items, sizeof(accx_bitmap_item) * g->items_cap));
+  if (!g->d_icnt) {
+    ACCX_CUDA_TRY(cudaMalloc(&g->d_icnt, sizeof(unsigned long long) * (n + 1)));
+    ACCX_CUDA_TRY(cudaMalloc(&g->d_prefix, sizeof(unsigned long long) * (n + 1)));
+    size_t bytes = 0;
+    ACCX_CUDA_TRY(cub::DeviceScan::ExclusiveSum(nullptr, bytes, g->d_icnt, g->d_prefix, (int64_t)n + 1));
+    ACCX_CUDA_TRY(cudaMalloc(&g->d_scan_tmp, bytes ? bytes : 16));
+    g->scan_tmp_bytes = bytes;
   }
   if (!g->d_counters) {
     // counters followed by the per-vertex bitmap work array
@@ -391,7 +632,8 @@ int accx_ensure_count_scratch(accx_graph *g) {
 
 // Tuned defaults (overridable per call).
 static int g_block_warps = 32;
-static int g_window_kb = 192;
+static int g_dense_kb = 128;
+static int g_sparse_kb = 64;
 
 
 static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s) {
@@ -399,9 +641,15 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s)
   int policy = o ? o->policy : ACCX_POLICY_HEURISTIC;
   int32_t bias = o ? o->bias : 0;
   int warps = (o && o->block_warps > 0) ? o->block_warps : g_block_warps;
-  int wkb = (o && o->bitmap_window_kb > 0) ? o->bitmap_window_kb : g_window_kb;
+  int dkb = (o && o->bitmap_window_kb > 0) ? o->bitmap_window_kb : g_dense_kb;
+  int skb = (o && o->sparse_table_kb > 0) ? o->sparse_table_kb : g_sparse_kb;
   if (policy < ACCX_POLICY_HEURISTIC || policy > ACCX_POLICY_MODEL) return ACCX_ERR_INVALID_ARG;
-  if (warps < 1 || warps > 32 || wkb < 1 || wkb > 224) return ACCX_ERR_INVALID_ARG;
+  if (warps < 1 || warps > 32 || dkb < 1 || skb < 1 || dkb + skb > 200) return ACCX_ERR_INVALID_ARG;
+  if (n == 0) {
+    g->cnt_bias = bias;
+    g->cnt_valid = true;
+    return ACCX_OK;
+  }
   int rc = accx_ensure_count_scratch(g);
   if (rc) return rc;
   if (policy == ACCX_POLICY_TABLE) {
@@ -417,10 +665,15 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s)
     ACCX_CUDA_TRY(cudaMemcpyAsync(g->d_table, t, ACCX_NB * ACCX_NB, cudaMemcpyHostToDevice, s));
     ACCX_CUDA_TRY(cudaStreamSynchronize(s));
   }
+  // counting runs on the relabeled CSR when the handle has one
+  const bool rel = g->d_roff != nullptr;
+  const uint32_t *off = rel ? g->d_roff : g->d_off;
+  const int32_t *dst = rel ? g->d_rdst : g->d_dst;
+  int32_t *cnt = rel ? g->d_rcnt : g->d_cnt;
   unsigned long long *ctr = g->d_counters;
   unsigned long long *work_u = g->d_counters + C_NUM;
-  ACCX_CUDA_TRY(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long) * C_NUM, s));
-  ACCX_CUDA_TRY(cudaMemsetAsync(g->d_cnt, 0, sizeof(int32_t) * (size_t)(m ? m : 1), s));
+  ACCX_CUDA_TRY(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long) * (C_NUM + (size_t)n + 1), s));
+  ACCX_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (size_t)(m ? m : 1), s));
   if (m == 0) {
     g->cnt_bias = bias;
     g->cnt_valid = true;
@@ -435,25 +688,32 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s)
 #define ACCX_MARK(i) \
   if (timing) ACCX_CUDA_TRY(cudaEventRecord(g->ev[i], s));
   ACCX_MARK(0);
-  k_classify<256><<<tiles, 256, 0, s>>>(g->d_off, g->d_dst, n, m, policy, g->d_table, g->d_edge_list, list_cap,
-                                        work_u, ctr);
+  k_classify<256><<<tiles, 256, 0, s>>>(off, dst, n, m, policy, g->d_table, g->d_edge_list, list_cap, work_u, ctr);
   const int sms = accx_sm_count(g->device);
-  k_make_items<<<sms * 4, 256, 0, s>>>(g->d_off, n, work_u, g->d_items, g->items_cap, ITEM_TARGET_DEFAULT, ctr);
+  const uint32_t W = (uint32_t)dkb * 8192u;        // dense ids (bits)
+  const uint32_t S = (uint32_t)skb * 1024u / 8u;   // sparse 8-byte slots
+  const size_t smem = (size_t)W / 8u + (size_t)S * 8u;
+  const uint32_t target = ITEM_TARGET_DEFAULT;
+  k_item_counts<<<sms * 4, 256, 0, s>>>(off, dst, n, work_u, W, S / 2, target, g->d_icnt, ctr);
+  ACCX_CUDA_TRY(cub::DeviceScan::ExclusiveSum(g->d_scan_tmp, g->scan_tmp_bytes, g->d_icnt, g->d_prefix,
+                                              (int64_t)n + 1, s));
   ACCX_MARK(1);
-  k_merge<<<sms * 8, MERGE_WARPS * 32, 0, s>>>(g->d_off, g->d_dst, g->d_edge_list, list_cap, ctr, g->d_cnt);
+  k_merge<<<sms * 8, MERGE_WARPS * 32, 0, s>>>(off, dst, g->d_edge_list, list_cap, ctr, cnt);
   ACCX_MARK(2);
-  k_gallop<<<sms * 8, MERGE_WARPS * 32, 0, s>>>(g->d_off, g->d_dst, g->d_edge_list, list_cap, ctr, g->d_cnt);
+  k_gallop<<<sms * 8, MERGE_WARPS * 32, 0, s>>>(off, dst, g->d_edge_list, list_cap, ctr, cnt);
   ACCX_MARK(3);
-  const uint32_t win_words = (uint32_t)wkb * 256u;  // KiB -> 32-bit words
-  const size_t smem = (size_t)win_words * 4u;
   ACCX_CUDA_TRY(cudaFuncSetAttribute(k_bitmap, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
   ACCX_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bitmap, warps * 32, smem));
   if (per_sm < 1) return ACCX_ERR_INVALID_ARG;
-  k_bitmap<<<sms * per_sm, warps * 32, smem, s>>>(g->d_off, g->d_dst, policy, g->d_table, g->d_items, g->items_cap, ctr,
-                                                  win_words, g->d_cnt);
+  k_bitmap<<<sms * per_sm, warps * 32, smem, s>>>(off, dst, n, policy, g->d_table, work_u, g->d_prefix, W, S, target,
+                                                  cnt);
   ACCX_MARK(4);
-  k_mirror<256><<<tiles, 256, 0, s>>>(g->d_off, g->d_dst, n, m, bias, g->d_cnt);
+  k_mirror<256><<<tiles, 256, 0, s>>>(off, dst, n, m, bias, cnt);
+  if (rel) {
+    rc = accx_relabel_gather(g, s);
+    if (rc) return rc;
+  }
   ACCX_MARK(5);
 #undef ACCX_MARK
   ACCX_CUDA_TRY(cudaGetLastError());

@@ -250,10 +250,10 @@ extern "C" int accx_graph_load_dir(const char *dir, unsigned flags, void *stream
 
 extern "C" int accx_graph_free(accx_graph *g) {
   if (!g) return ACCX_ERR_INVALID_ARG;
-  void *ptrs[] = {g->d_off,       g->d_dst,   g->d_cnt,       g->d_edge_list, g->d_items,
+  void *ptrs[] = {g->d_off,       g->d_dst,   g->d_cnt,       g->d_edge_list, g->d_icnt, g->d_prefix, g->d_scan_tmp,
                   g->d_counters,  g->d_table, g->d_simbits,   g->d_core_count, g->d_label,
                   g->d_parent,    g->d_hubmin, g->d_hubmax,   g->d_qcounters,  g->d_pairs,
-                  g->d_pairs_tmp};
+                  g->d_pairs_tmp, g->d_roff, g->d_rdst, g->d_rmap, g->d_rcnt, g->d_oldid, g->d_newid};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i <= ACCX_NUM_PHASES; i++)

@@ -158,8 +158,11 @@ def pick_policy(G, args):
         return "bitmap", {"note": "cost model unavailable: %s" % e}
 
 
-def time_counts(G, policy, table, steps, warmup, stream, world, timing=True):
+def time_counts(G, policy, table, steps, warmup, tstream, world, timing=True):
+    """K counts back to back on `tstream` (a torch.cuda.Stream, also handed to
+    the library), bracketed by CUDA events on that stream."""
     import torch
+    stream = tstream.cuda_stream
     for _ in range(warmup):
         G.count(policy=policy, table=table, out=None, stream=stream)
     torch.cuda.synchronize()
@@ -168,13 +171,13 @@ def time_counts(G, policy, table, steps, warmup, stream, world, timing=True):
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     phases = {}
-    ev0.record(stream)
+    ev0.record(tstream)
     for _ in range(steps):
         G.count(policy=policy, table=table, out=None, stream=stream, timing=timing)
         if timing:
             for k, v in G.timings().items():
                 phases[k] = phases.get(k, 0.0) + v
-    ev1.record(stream)
+    ev1.record(tstream)
     torch.cuda.synchronize()
     barrier(world)
     torch.cuda.synchronize()
@@ -271,11 +274,11 @@ def run_gb300(args):
     bit_exact = bool(np.array_equal(a, b))
     del a, b
     with ClockSampler(local) as clk:
-        ms, phases = time_counts(G, policy, table, args.steps, args.warmup, sp, world)
+        ms, phases = time_counts(G, policy, table, args.steps, args.warmup, stream, world)
     ms = max_over_ranks(ms, world)
     stats = G.last_stats()
     owner_work = G.owner_work()
-    plain_ms, plain_phases = time_counts(G, "heuristic", None, args.steps, args.warmup, sp, world)
+    plain_ms, plain_phases = time_counts(G, "heuristic", None, args.steps, args.warmup, stream, world)
     plain_ms = max_over_ranks(plain_ms, world)
     total_m = sum_over_ranks(G.m, world)
     value = total_m / (ms / 1e3) / 1e9

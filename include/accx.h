@@ -75,6 +75,14 @@ int accx_graph_load_dir(const char *dir, unsigned flags, void *stream, accx_grap
 int accx_graph_free(accx_graph *g);
 int accx_graph_size(const accx_graph *g, uint32_t *n, uint64_t *m);
 
+/* Builds (once) a degree-descending relabeled copy of the CSR on the device,
+ * the GPU form of the reference's "deg" reorder (scan-query/scan_xp.cpp:1145-1222,
+ * :1279-1301).  Later counts run on it and are mapped back to the handle's entry
+ * order, so results are unchanged; the shared-memory bitmap then serves most
+ * probes from its dense low-id window.  Costs 4*(n+1) + 12*m bytes of HBM. */
+int accx_graph_relabel(accx_graph *g, void *stream);
+int accx_graph_is_relabeled(const accx_graph *g);
+
 /* Copies the CSR back (host or device destination pointers). */
 int accx_graph_download(const accx_graph *g, uint32_t *off, int32_t *dst, void *stream);
 
@@ -129,8 +137,9 @@ typedef struct {
   const uint8_t *table;   /* ACCX_NB*ACCX_NB kinds, row = owner bucket; for ACCX_POLICY_TABLE */
   int32_t bias;           /* added to every count; 2 gives the reference's common_node_num */
   int block_warps;        /* bitmap/merge CTA size in warps (0 = tuned default) */
-  int bitmap_window_kb;   /* shared-memory bitmap window in KiB (0 = tuned default) */
+  int bitmap_window_kb;   /* dense shared-memory bitmap over the lowest ids, KiB (0 = tuned default) */
   int timing;             /* 1: record CUDA events around each phase (accx_cn_last_timings) */
+  int sparse_table_kb;    /* hashed bitmap-word table for the other ids, KiB (0 = tuned default) */
 } accx_count_opts;
 
 /* Counts cnt[e] = |N(u) ∩ N(v)| + bias for every CSR entry e=(u,v) into the

@@ -33,8 +33,15 @@ def test_counts_match_reference_all_policies(name):
         assert np.array_equal(cnt, g["cnn"]), pol
     cnt = G.count(policy="table", table=_table(1), bias=2)
     assert np.array_equal(cnt, g["cnn"])
-    # tiny bitmap windows: 1 KiB = 8192 ids per window, many windows per owner
-    cnt = G.count(policy="bitmap", bias=2, window_kb=1, block_warps=4)
+    # tiny shared tables: an 8192-id dense window and a 128-slot sparse table
+    # (chunks of 64 ids), so owners are cut into many chunks
+    cnt = G.count(policy="bitmap", bias=2, window_kb=1, sparse_kb=1, block_warps=4)
+    assert np.array_equal(cnt, g["cnn"])
+    G.relabel()
+    assert G.relabeled
+    for pol in POLICIES:
+        assert np.array_equal(G.count(policy=pol, bias=2), g["cnn"]), pol
+    cnt = G.count(policy="bitmap", bias=2, window_kb=1, sparse_kb=1, block_warps=8)
     assert np.array_equal(cnt, g["cnn"])
     raw = G.count(policy="heuristic", bias=0)
     assert np.array_equal(raw + 2, g["cnn"])
@@ -83,6 +90,9 @@ def test_rmat16_full_parity_with_oracle(eps, mu, tmp_path):
     ref = oracle.scan(off, dst, eps, mu, nthreads=8, out_dir=str(tmp_path))
     for pol in POLICIES:
         assert np.array_equal(G.count(policy=pol, bias=2), ref["cnn"]), pol
+    G.relabel()
+    assert np.array_equal(G.count(policy="bitmap", bias=2), ref["cnn"])
+    assert np.array_equal(G.count(policy="bitmap", bias=2, window_kb=2, sparse_kb=2), ref["cnn"])
     r = G.scan(eps, mu)
     assert np.array_equal(r["sim"], ref["sim"])
     assert np.array_equal(r["label"], ref["label"])
@@ -103,6 +113,9 @@ def test_chung_lu_skew_parity_with_oracle():
     ref = oracle.cn_count(off, dst, nthreads=8)
     for pol in POLICIES:
         assert np.array_equal(G.count(policy=pol, bias=2), ref), pol
+    G.relabel()
+    for pol in POLICIES:
+        assert np.array_equal(G.count(policy=pol, bias=2), ref), pol
 
 
 def test_large_rmat_policies_agree_and_are_symmetric():
@@ -114,6 +127,9 @@ def test_large_rmat_policies_agree_and_are_symmetric():
     base = G.count(policy="heuristic")
     for pol in ["merge", "bitmap", "gallop"]:
         assert np.array_equal(G.count(policy=pol), base), pol
+    G.relabel()
+    assert np.array_equal(G.count(policy="bitmap"), base)
+    assert np.array_equal(G.count(policy="bitmap", window_kb=16, sparse_kb=4), base)
     n = len(off) - 1
     src = np.repeat(np.arange(n, dtype=np.int64), np.diff(off).astype(np.int64))
     key = src * n + dst

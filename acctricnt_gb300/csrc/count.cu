@@ -25,6 +25,7 @@
 
 #include "accx_internal.h"
 #include "devutil.cuh"
+#include "merge.cuh"
 
 // counters layout
 #define C_MERGE 0
@@ -35,7 +36,6 @@
 #define C_OWNER 9  // + kind: owner-side elements
 #define C_NUM 16
 
-#define MERGE_WIN 128        // int32 per list window (32 lanes x uint4)
 #define MERGE_WARPS 8        // warps per merge/gallop CTA
 #define ITEM_TARGET_DEFAULT (1u << 20)  // probe elements per bitmap work item
 
@@ -116,80 +116,6 @@ __global__ void __launch_bounds__(TILE) k_classify(const uint32_t *__restrict__ 
 }
 
 // ---------------------------------------------------------------------------
-// Warp merge-path intersection.
-//
-// Each list is consumed in windows of 128 ids loaded by the 32 lanes as 16-byte
-// vectors from 16-byte aligned addresses (the first window of a list starts at
-// the list's first entry and may be shorter).  A window pair is intersected by
-// merge path: every lane takes an equal share of the merged order (a binary
-// search on its diagonal), walks it, and counts B[j] when the A element just
-// before it in merged order (ties take A first) equals it.  The window whose last
-// id is smaller is then replaced (both on equality); matches cannot straddle a
-// replaced window, so every common id is counted exactly once.
-__device__ __forceinline__ int accx_load_window(const int32_t *__restrict__ dst, uint32_t pos, uint32_t end,
-                                                int32_t *__restrict__ buf, int lane) {
-  uint32_t al = pos & ~3u;
-  uint32_t idx = al + 4u * (uint32_t)lane;
-  if (idx < end && idx + 4u > pos) {
-    int4 q = __ldg(reinterpret_cast<const int4 *>(dst + idx));
-    int32_t vals[4] = {q.x, q.y, q.z, q.w};
-#pragma unroll
-    for (int t = 0; t < 4; t++) {
-      uint32_t ii = idx + (uint32_t)t;
-      if (ii >= pos && ii < end) buf[ii - pos] = vals[t];
-    }
-  }
-  uint32_t lim = al + MERGE_WIN;
-  if (lim > end) lim = end;
-  return (int)(lim - pos);
-}
-
-__device__ __forceinline__ uint32_t accx_warp_merge_count(const int32_t *__restrict__ dst, uint32_t ab, uint32_t ae,
-                                                          uint32_t bb, uint32_t be, int32_t *__restrict__ A,
-                                                          int32_t *__restrict__ B, int lane) {
-  uint32_t c = 0;
-  if (ab >= ae || bb >= be) return 0;
-  int la = accx_load_window(dst, ab, ae, A, lane);
-  int lb = accx_load_window(dst, bb, be, B, lane);
-  __syncwarp();
-  for (;;) {
-    int32_t a_first = A[0], a_last = A[la - 1], b_first = B[0], b_last = B[lb - 1];
-    if (a_last >= b_first && b_last >= a_first) {
-      int total = la + lb;
-      int chunk = (total + 31) >> 5;
-      int d0 = min(lane * chunk, total), d1 = min(d0 + chunk, total);
-      int lo = max(0, d0 - lb), hi = min(d0, la);
-      while (lo < hi) {
-        int mid = (lo + hi) >> 1;
-        if (A[mid] <= B[d0 - mid - 1]) lo = mid + 1; else hi = mid;
-      }
-      int i = lo, j = d0 - lo;
-      for (int d = d0; d < d1; d++) {
-        if (i < la && (j >= lb || A[i] <= B[j])) {
-          i++;
-        } else {
-          if (i > 0 && A[i - 1] == B[j]) c++;
-          j++;
-        }
-      }
-    }
-    bool adv_a = a_last <= b_last, adv_b = b_last <= a_last;
-    __syncwarp();
-    if (adv_a) {
-      ab += (uint32_t)la;
-      if (ab >= ae) break;
-      la = accx_load_window(dst, ab, ae, A, lane);
-    }
-    if (adv_b) {
-      bb += (uint32_t)lb;
-      if (bb >= be) break;
-      lb = accx_load_window(dst, bb, be, B, lane);
-    }
-    __syncwarp();
-  }
-  return __reduce_add_sync(ACCX_FULL_MASK, c);
-}
-
 __global__ void __launch_bounds__(MERGE_WARPS * 32) k_merge(const uint32_t *__restrict__ off,
                                                              const int32_t *__restrict__ dst,
                                                              const uint2 *__restrict__ list, uint32_t list_cap,

@@ -73,6 +73,8 @@ def _load():
         "accx_write_graph_dir": (C.c_int, [C.c_char_p, P, P, C.c_uint32, C.c_uint64]),
         "accx_cn_count": (C.c_int, [P, C.POINTER(CountOpts), P, P]),
         "accx_cn_last_stats": (C.c_int, [P, P, P]),
+        "accx_cn_count_noalloc": (C.c_int, [P, P, C.c_uint32, C.c_uint64, C.c_int32, P, P]),
+        "accx_cn_count_noalloc_max_entries": (C.c_uint64, []),
         "accx_cn_last_owner_work": (C.c_int, [P, P]),
         "accx_cn_last_timings": (C.c_int, [P, P]),
         "accx_scan_query": (C.c_int, [P, C.c_double, C.c_int, P, P, P, C.POINTER(ScanSummary), P]),
@@ -160,6 +162,16 @@ def similar_exact_batch(cnn, du, dv, eps):
     _check(lib.accx_similar_exact_batch(len(cnn), _ptr(cnn), _ptr(du), _ptr(dv), float(eps), _ptr(out)),
            "similar_exact_batch")
     return out[:len(cnn)].astype(bool)
+
+
+def cn_count_noalloc(off_ptr, dst_ptr, n, m, bias, cnt_ptr, stream=None):
+    """accx_cn_count_noalloc on device pointers (no memory is allocated)."""
+    _check(lib.accx_cn_count_noalloc(C.c_void_p(off_ptr), C.c_void_p(dst_ptr), int(n), int(m), int(bias),
+                                     C.c_void_p(cnt_ptr), _stream_ptr(stream)), "cn_count_noalloc")
+
+
+def cn_count_noalloc_max_entries():
+    return int(lib.accx_cn_count_noalloc_max_entries())
 
 
 def _stream_ptr(stream):

@@ -165,6 +165,24 @@ int accx_cn_last_owner_work(const accx_graph *g, uint64_t owner_work[ACCX_NUM_KI
 /* Milliseconds per phase of the last timed count (waits for it to finish). */
 int accx_cn_last_timings(const accx_graph *g, float ms[ACCX_NUM_PHASES]);
 
+/* All-edge counts without allocating any memory.  (No counterpart in the
+ * reference: it exists for callers that cannot call cudaMalloc -- a plugin in a
+ * process whose framework owns every byte of device memory, code under a
+ * stream-ordered pool budget, or a loop that must never enter the driver's
+ * allocator.)  off/dst/cnt are device pointers: a symmetric CSR as
+ * accx_graph_create accepts it, and the int32 output, cnt[e] = |N(u) ∩ N(v)| +
+ * bias for every entry.  The only scratch is a fixed 8 MiB array inside the
+ * library that every GPU loading the library keeps until the process exits, so
+ * graphs are limited to accx_cn_count_noalloc_max_entries() CSR entries (2^21);
+ * larger ones get ACCX_ERR_TOO_LARGE, host pointers ACCX_ERR_INVALID_ARG.  The
+ * first call on a device looks up that array's device address (make it before
+ * any stream capture on that device).  All calls share the array: calls that
+ * overlap on the GPU (other streams, other threads) race and must be ordered by
+ * the caller. */
+int accx_cn_count_noalloc(const uint32_t *off, const int32_t *dst, uint32_t n, uint64_t m, int32_t bias,
+                          int32_t *cnt, void *stream);
+uint64_t accx_cn_count_noalloc_max_entries(void);
+
 /* ---- SCAN query ------------------------------------------------------------- */
 #define ACCX_UNCLASSIFIED 0
 #define ACCX_CORE 1

@@ -18,6 +18,7 @@ HOST = os.path.join(PKG, "host")
 BUILD = os.path.join(PKG, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 LIB = os.path.join(BUILD, "libaccx.so")
+CLIS = {"scan-xp-gb300": "main_scanxp.cpp", "scan-xp-gb300-varying": "main_scanxp_varying.cpp"}
 CLI = os.path.join(BUILD, "scan-xp-gb300")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -69,13 +70,16 @@ def build(verbose=False):
     if not os.path.exists(LIB) or os.path.getmtime(LIB) < _newest(objs):
         cmd = [_nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lpthread"]
         subprocess.run(cmd, check=True)
-    host_srcs = sorted(glob.glob(os.path.join(HOST, "*.cpp")))
-    host_hdrs = glob.glob(os.path.join(HOST, "*.h"))
-    if host_srcs and (not os.path.exists(CLI) or os.path.getmtime(CLI) < max(_newest(host_srcs + host_hdrs),
-                                                                             os.path.getmtime(LIB))):
-        cmd = ["g++", "-O2", "-std=c++17", "-fopenmp", "-I" + INCLUDE, "-I" + HOST] + host_srcs + \
-            ["-L" + BUILD, "-laccx", "-Wl,-rpath,$ORIGIN", "-o", CLI]
-        subprocess.run(cmd, check=True)
+    mains = set(CLIS.values())
+    common = sorted(p for p in glob.glob(os.path.join(HOST, "*.cpp")) if os.path.basename(p) not in mains)
+    host_hdrs = glob.glob(os.path.join(HOST, "*.h")) + [os.path.join(INCLUDE, "accx.h")]
+    for exe, main in CLIS.items():
+        out = os.path.join(BUILD, exe)
+        srcs = common + [os.path.join(HOST, main)]
+        if not os.path.exists(out) or os.path.getmtime(out) < max(_newest(srcs + host_hdrs), os.path.getmtime(LIB)):
+            cmd = ["g++", "-O2", "-std=c++17", "-I" + INCLUDE, "-I" + HOST] + srcs + \
+                ["-L" + BUILD, "-laccx", "-Wl,-rpath,$ORIGIN", "-o", out]
+            subprocess.run(cmd, check=True)
     if verbose:
         print("built", LIB)
     return LIB

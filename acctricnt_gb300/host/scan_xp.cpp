@@ -1,0 +1,135 @@
+// SCAN_XP on libaccx: the reference's Execute() sequence
+// (scan-query-cuda/scan_xp_common.cu:334-360), each phase one or two C ABI calls.
+#include "scan_xp.h"
+
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#include <chrono>
+#include <stdexcept>
+#include <string>
+
+static FILE *g_log_file = nullptr;
+
+void accx_log_set_file(const char *path) {
+  if (g_log_file) fclose(g_log_file);
+  g_log_file = path ? fopen(path, "a+") : nullptr;
+}
+
+void accx_log(const char *fmt, ...) {
+  char msg[2048];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(msg, sizeof(msg), fmt, ap);
+  va_end(ap);
+  time_t t = time(nullptr);
+  char ts[32];
+  strftime(ts, sizeof(ts), "%H:%M:%S", localtime(&t));
+  printf("%s INFO %s\n", ts, msg);
+  fflush(stdout);
+  if (g_log_file) {
+    fprintf(g_log_file, "%s INFO %s\n", ts, msg);
+    fflush(g_log_file);
+  }
+}
+
+static void check(int rc, const char *what) {
+  if (rc != ACCX_OK) throw std::runtime_error(std::string(what) + ": " + accx_strerror(rc));
+}
+
+ScanXpOptions ScanXpOptions::from_env() {
+  ScanXpOptions o;
+  const char *p = getenv("ACCX_POLICY");
+  if (p) {
+    std::string s(p);
+    if (s == "heuristic") o.policy = ACCX_POLICY_HEURISTIC;
+    else if (s == "merge") o.policy = ACCX_POLICY_MERGE;
+    else if (s == "gallop") o.policy = ACCX_POLICY_GALLOP;
+    else if (s == "bitmap") o.policy = ACCX_POLICY_BITMAP;
+    else if (s == "model") o.policy = ACCX_POLICY_MODEL;
+    else o.policy = ACCX_POLICY_TABLE;
+  }
+  const char *r = getenv("ACCX_RELABEL");
+  if (r) o.relabel = atoi(r) != 0;
+  return o;
+}
+
+// Default bucket table: galloping where the owner's degree bucket exceeds the
+// other's by 6 or more (ratio >= 64), the shared-memory bitmap for owners of
+// degree >= 256, warp merge below.
+static void default_table(uint8_t *t) {
+  for (int a = 0; a < ACCX_NB; a++)
+    for (int b = 0; b < ACCX_NB; b++)
+      t[a * ACCX_NB + b] = a >= 8 ? ACCX_KIND_BITMAP : (a - b >= 6 ? ACCX_KIND_GALLOP : ACCX_KIND_MERGE);
+}
+
+using clk = std::chrono::steady_clock;
+static double secs(clk::time_point a) { return std::chrono::duration<double>(clk::now() - a).count(); }
+
+SCAN_XP::SCAN_XP(int thread_num, int min_u, double epsilon, char *dir)
+    : SCAN_XP(thread_num, min_u, epsilon, dir, ScanXpOptions::from_env()) {}
+
+SCAN_XP::SCAN_XP(int thread_num, int min_u, double epsilon, char *dir, const ScanXpOptions &opts)
+    : min_u_(min_u), epsilon_(epsilon), dir_(dir ? dir : ""), opts_(opts), thread_num_(thread_num) {
+  auto t0 = clk::now();
+  check(accx_graph_load_dir(dir_.c_str(), ACCX_GRAPH_VALIDATE, nullptr, &g_), "load graph");
+  uint32_t n = 0;
+  uint64_t m = 0;
+  accx_graph_size(g_, &n, &m);
+  accx_log("graph dir: %s", dir_.c_str());
+  accx_log("thread num: %d", thread_num_);
+  accx_log("graph, n: %u, m: %llu (loaded and checked in %.3lf s)", n, (unsigned long long)m, secs(t0));
+  if (opts_.relabel) {
+    t0 = clk::now();
+    check(accx_graph_relabel(g_, nullptr), "relabel");
+    accx_log("PreProcess Reordering Cost (GPU degree-descending): %.3lf s", secs(t0));
+  }
+}
+
+SCAN_XP::~SCAN_XP() {
+  if (g_) accx_graph_free(g_);
+}
+
+void SCAN_XP::CheckCore() {
+  uint8_t table[ACCX_NB * ACCX_NB];
+  default_table(table);
+  accx_count_opts o;
+  memset(&o, 0, sizeof(o));
+  o.policy = opts_.policy;
+  o.table = table;
+  o.bias = 2;  // common_node_num = 2 + |N(u) ∩ N(v)|
+  o.block_warps = opts_.block_warps;
+  auto t0 = clk::now();
+  check(accx_cn_count(g_, &o, nullptr, nullptr), "count");
+  check(accx_scan_query(g_, epsilon_, min_u_, nullptr, nullptr, nullptr, &summary, nullptr), "similarity");
+  accx_log("All-Edge CN-Cnt + core checking (GPU): %.3lf s", secs(t0));
+}
+
+void SCAN_XP::ClusterCore() {
+  // union-find, hubs and outliers ran with the query; report as the reference does
+  accx_log("Core: %u", summary.cores);
+}
+
+void SCAN_XP::PostProcess() {
+  accx_log("Cluster: %u, Hub: %u, Outlier: %u", summary.clusters, summary.hubs, summary.outliers);
+}
+
+void SCAN_XP::PrepareResultOutput() {
+  auto t0 = clk::now();
+  check(accx_write_result(g_, dir_.c_str(), epsilon_, min_u_, nullptr), "write result");
+  accx_log("Step4 - output to the disk cost: %.3lf s", secs(t0));
+}
+
+void SCAN_XP::Execute() {
+  auto t0 = clk::now();
+  CheckCore();
+  accx_log("Step1 - CheckCore: %.3lf s", secs(t0));
+  t0 = clk::now();
+  ClusterCore();
+  accx_log("Step2 - ClusterCore: %.3lf s", secs(t0));
+  PostProcess();
+  PrepareResultOutput();
+}

@@ -24,6 +24,9 @@ POLICY_HEURISTIC, POLICY_TABLE, POLICY_MERGE, POLICY_GALLOP, POLICY_BITMAP, POLI
 POLICIES = {"heuristic": POLICY_HEURISTIC, "table": POLICY_TABLE, "merge": POLICY_MERGE,
             "gallop": POLICY_GALLOP, "bitmap": POLICY_BITMAP, "model": POLICY_MODEL}
 NB = 24
+KIND_SKIP = 3
+MODEL_IN, MODEL_H, MODEL_OUT = 8, 32, 3
+MODEL_NPARAMS = MODEL_IN * MODEL_H + MODEL_H + MODEL_H * MODEL_H + MODEL_H + MODEL_H * MODEL_OUT + MODEL_OUT
 PHASES = ("plan", "merge", "gallop", "bitmap", "mirror")
 UNCLASSIFIED, CORE, HUB = 0, 1, 2
 
@@ -82,6 +85,17 @@ def _load():
         "accx_eps_string": (C.c_int, [C.c_double, C.c_char_p, C.c_size_t]),
         "accx_write_result": (C.c_int, [P, C.c_char_p, C.c_double, C.c_int, P]),
         "accx_similar_exact": (C.c_int, [C.c_uint32, C.c_uint32, C.c_uint32, C.c_double]),
+        "accx_model_create": (C.c_int, [C.c_uint64, C.POINTER(P)]),
+        "accx_model_free": (C.c_int, [P]),
+        "accx_model_get_params": (C.c_int, [P, P]),
+        "accx_model_set_params": (C.c_int, [P, P]),
+        "accx_bucket_stats": (C.c_int, [P, P, P, P]),
+        "accx_bucket_features": (C.c_int, [P, P]),
+        "accx_model_loss_grad": (C.c_int, [P, P, P, P, C.c_uint32, P, P]),
+        "accx_model_train": (C.c_int, [P, P, P, P, C.c_uint32, C.c_int, C.c_float, P]),
+        "accx_model_predict": (C.c_int, [P, P, C.c_uint32, P]),
+        "accx_model_table_for": (C.c_int, [P, P, P]),
+        "accx_graph_set_model": (C.c_int, [P, P]),
         "accx_similar_exact_batch": (C.c_int, [C.c_uint64, P, P, P, C.c_double, P]),
     }
     for name, (res, args) in sigs.items():
@@ -297,6 +311,22 @@ class Graph:
         _check(lib.accx_cn_last_timings(self._h, _ptr(ms)), "cn_last_timings")
         return dict(zip(PHASES, (float(x) for x in ms)))
 
+    def bucket_stats(self):
+        e = np.zeros(NB * NB, np.uint64)
+        so = np.zeros(NB * NB, np.float64)
+        sp = np.zeros(NB * NB, np.float64)
+        _check(lib.accx_bucket_stats(self._h, _ptr(e), _ptr(so), _ptr(sp)), "bucket_stats")
+        return e, so, sp
+
+    def bucket_features(self):
+        x = np.zeros((NB * NB, MODEL_IN), np.float32)
+        _check(lib.accx_bucket_features(self._h, _ptr(x)), "bucket_features")
+        return x
+
+    def set_model(self, model):
+        self._model = model  # keep the model alive while attached
+        _check(lib.accx_graph_set_model(self._h, model._h if model else None), "graph_set_model")
+
     def scan(self, eps, mu, want_sim=True, want_label=True, want_cluster=True, stream=None):
         sim = np.zeros(max(self.m, 1), np.uint8) if want_sim else None
         lab = np.zeros(max(self.n, 1), np.int32) if want_label else None
@@ -316,3 +346,60 @@ class Graph:
 
     def write_result(self, path, eps, mu, stream=None):
         _check(lib.accx_write_result(self._h, path.encode(), float(eps), int(mu), _stream_ptr(stream)), "write_result")
+
+
+class Model:
+    """The MLP cost model (accx_model): FP16 weights on the device."""
+
+    def __init__(self, seed=1):
+        self._h = C.c_void_p()
+        _check(lib.accx_model_create(int(seed), C.byref(self._h)), "model_create")
+
+    def __del__(self):
+        try:
+            if self._h:
+                lib.accx_model_free(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+    def params(self):
+        p = np.zeros(MODEL_NPARAMS, np.float32)
+        _check(lib.accx_model_get_params(self._h, _ptr(p)), "model_get_params")
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == MODEL_NPARAMS
+        _check(lib.accx_model_set_params(self._h, _ptr(p)), "model_set_params")
+
+    @staticmethod
+    def _samples(x, kind, target):
+        return (np.ascontiguousarray(x, np.float32).reshape(-1, MODEL_IN), np.ascontiguousarray(kind, np.int32),
+                np.ascontiguousarray(target, np.float32))
+
+    def loss_grad(self, x, kind, target):
+        x, kind, target = self._samples(x, kind, target)
+        g = np.zeros(MODEL_NPARAMS, np.float32)
+        loss = C.c_float()
+        _check(lib.accx_model_loss_grad(self._h, _ptr(x), _ptr(kind), _ptr(target), len(kind), _ptr(g),
+                                        C.byref(loss)), "model_loss_grad")
+        return float(loss.value), g
+
+    def train(self, x, kind, target, epochs=2000, lr=3e-3):
+        x, kind, target = self._samples(x, kind, target)
+        loss = C.c_float()
+        _check(lib.accx_model_train(self._h, _ptr(x), _ptr(kind), _ptr(target), len(kind), int(epochs), float(lr),
+                                    C.byref(loss)), "model_train")
+        return float(loss.value)
+
+    def predict(self, x):
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, MODEL_IN)
+        y = np.zeros((len(x), MODEL_OUT), np.float32)
+        _check(lib.accx_model_predict(self._h, _ptr(x), len(x), _ptr(y)), "model_predict")
+        return y
+
+    def table_for(self, graph):
+        t = np.zeros(NB * NB, np.uint8)
+        _check(lib.accx_model_table_for(self._h, graph._h, _ptr(t)), "model_table_for")
+        return t.reshape(NB, NB)

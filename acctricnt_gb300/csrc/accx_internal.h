@@ -95,6 +95,7 @@ int accx_ensure_count_scratch(accx_graph *g);
 // Cost-model state attached to a handle (model.cu).
 void accx_model_release(accx_graph *g);
 int accx_model_table(accx_graph *g, uint8_t *table);
+int accx_model_table_device(accx_graph *g, cudaStream_t s);
 
 // Exclusive/inclusive helpers implemented in gen.cu.
 // Relabeled counts -> the handle's entry order (relabel.cu).

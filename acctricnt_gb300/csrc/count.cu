@@ -581,15 +581,12 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s)
   if (policy == ACCX_POLICY_TABLE) {
     if (!o->table) return ACCX_ERR_INVALID_ARG;
     for (int i = 0; i < ACCX_NB * ACCX_NB; i++)
-      if (o->table[i] >= ACCX_NUM_KINDS) return ACCX_ERR_INVALID_ARG;
+      if (o->table[i] > ACCX_KIND_SKIP) return ACCX_ERR_INVALID_ARG;
     ACCX_CUDA_TRY(cudaMemcpyAsync(g->d_table, o->table, ACCX_NB * ACCX_NB, cudaMemcpyHostToDevice, s));
     ACCX_CUDA_TRY(cudaStreamSynchronize(s));  // o->table is pageable caller memory
   } else if (policy == ACCX_POLICY_MODEL) {
-    uint8_t t[ACCX_NB * ACCX_NB];
-    rc = accx_model_table(g, t);
+    rc = accx_model_table_device(g, s);  // the attached model writes g->d_table on the device
     if (rc) return rc;
-    ACCX_CUDA_TRY(cudaMemcpyAsync(g->d_table, t, ACCX_NB * ACCX_NB, cudaMemcpyHostToDevice, s));
-    ACCX_CUDA_TRY(cudaStreamSynchronize(s));
   }
   // counting runs on the relabeled CSR when the handle has one
   const bool rel = g->d_roff != nullptr;

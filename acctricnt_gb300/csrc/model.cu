@@ -1,7 +1,294 @@
-// Cost-model state attached to a graph handle (filled in by the model module).
-#include "accx_internal.h"
+// Learned kernel scheduler: a small MLP cost model per degree bucket.
+//
+// Network: ACCX_MODEL_IN features -> 32 ReLU -> 32 ReLU -> one output per
+// kernel kind (predicted log2 seconds per edge).  Parameters live on the device
+// as an FP32 master copy (updated by Adam) and the FP16 weights every forward
+// pass reads; all products accumulate in FP32.  The kernels here are the
+// library's own:
+//   k_model_grad     forward + backward of a batch (one thread per sample),
+//                    gradient summed in shared memory, then globally;
+//   k_model_adam     the optimizer step, refreshing the FP16 copy;
+//   k_model_infer    register-resident inference: a warp keeps one hidden unit's
+//                    weights per lane in registers for the whole launch and
+//                    evaluates rows with shuffles; with a graph's bucket features
+//                    it writes the argmin kind of every bucket straight into the
+//                    handle's kernel table, so ACCX_POLICY_MODEL needs no host
+//                    round trip.
+#include <cuda_fp16.h>
+#include <math.h>
+#include <string.h>
 
-extern "C" int accx_model_table_stub(void) { return 0; }
+#include <vector>
+
+#include "accx_internal.h"
+#include "devutil.cuh"
+
+#define IN ACCX_MODEL_IN
+#define H ACCX_MODEL_H
+#define OUT ACCX_MODEL_OUT
+#define NP ACCX_MODEL_NPARAMS
+#define O_W1 0
+#define O_B1 (IN * H)
+#define O_W2 (O_B1 + H)
+#define O_B2 (O_W2 + H * H)
+#define O_W3 (O_B2 + H)
+#define O_B3 (O_W3 + H * OUT)
+
+static_assert(O_B3 + OUT == NP, "parameter layout");
+
+struct accx_model {
+  int device = 0;
+  float *d_master = nullptr;  // NP fp32
+  __half *d_w = nullptr;      // NP fp16 (what the forward pass reads)
+  float *d_m = nullptr, *d_v = nullptr;  // Adam moments
+  float *d_grad = nullptr;    // NP
+  float *d_loss = nullptr;    // 1
+  int step = 0;
+};
+
+// ---------------------------------------------------------------------------
+__global__ void k_to_half(const float *__restrict__ src, __half *__restrict__ dst, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = __float2half_rn(src[i]);
+}
+
+// Forward + backward of the mean squared error on the output of each sample's
+// kind.  grad and loss are accumulated (the caller zeroes them).
+__global__ void __launch_bounds__(128) k_model_grad(const __half *__restrict__ w, const float *__restrict__ x,
+                                                    const int32_t *__restrict__ kind, const float *__restrict__ target,
+                                                    uint32_t k, float *__restrict__ grad, float *__restrict__ loss) {
+  __shared__ float sw[NP];
+  __shared__ float sg[NP];
+  __shared__ float sl;
+  for (int i = threadIdx.x; i < NP; i += blockDim.x) {
+    sw[i] = __half2float(w[i]);
+    sg[i] = 0.f;
+  }
+  if (threadIdx.x == 0) sl = 0.f;
+  __syncthreads();
+  const float inv = 1.f / (float)k;
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < k; s += gridDim.x * blockDim.x) {
+    float xi[IN], h1[H], h2[H];
+#pragma unroll
+    for (int f = 0; f < IN; f++) xi[f] = x[(size_t)s * IN + f];
+#pragma unroll
+    for (int j = 0; j < H; j++) {
+      float a = sw[O_B1 + j];
+#pragma unroll
+      for (int f = 0; f < IN; f++) a = fmaf(xi[f], sw[O_W1 + f * H + j], a);
+      h1[j] = a > 0.f ? a : 0.f;
+    }
+#pragma unroll
+    for (int j = 0; j < H; j++) {
+      float a = sw[O_B2 + j];
+#pragma unroll
+      for (int i = 0; i < H; i++) a = fmaf(h1[i], sw[O_W2 + i * H + j], a);
+      h2[j] = a > 0.f ? a : 0.f;
+    }
+    const int o = kind[s];
+    float y = sw[O_B3 + o];
+#pragma unroll
+    for (int j = 0; j < H; j++) y = fmaf(h2[j], sw[O_W3 + j * OUT + o], y);
+    const float err = y - target[s];
+    atomicAdd(&sl, err * err * inv);
+    const float dy = 2.f * err * inv;
+    atomicAdd(&sg[O_B3 + o], dy);
+    float dh2[H];
+#pragma unroll
+    for (int j = 0; j < H; j++) {
+      atomicAdd(&sg[O_W3 + j * OUT + o], h2[j] * dy);
+      dh2[j] = h2[j] > 0.f ? sw[O_W3 + j * OUT + o] * dy : 0.f;
+      atomicAdd(&sg[O_B2 + j], dh2[j]);
+    }
+#pragma unroll
+    for (int i = 0; i < H; i++) {
+      float d1 = 0.f;
+#pragma unroll
+      for (int j = 0; j < H; j++) {
+        atomicAdd(&sg[O_W2 + i * H + j], h1[i] * dh2[j]);
+        d1 = fmaf(sw[O_W2 + i * H + j], dh2[j], d1);
+      }
+      d1 = h1[i] > 0.f ? d1 : 0.f;
+      atomicAdd(&sg[O_B1 + i], d1);
+#pragma unroll
+      for (int f = 0; f < IN; f++) atomicAdd(&sg[O_W1 + f * H + i], xi[f] * d1);
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < NP; i += blockDim.x)
+    if (sg[i] != 0.f) atomicAdd(&grad[i], sg[i]);
+  if (threadIdx.x == 0) atomicAdd(loss, sl);
+}
+
+__global__ void k_model_adam(float *__restrict__ master, __half *__restrict__ w, float *__restrict__ mm,
+                             float *__restrict__ vv, const float *__restrict__ grad, float lr, float b1t, float b2t) {
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NP; i += gridDim.x * blockDim.x) {
+    float g = grad[i];
+    float m = b1 * mm[i] + (1.f - b1) * g;
+    float v = b2 * vv[i] + (1.f - b2) * g * g;
+    mm[i] = m;
+    vv[i] = v;
+    float mh = m / (1.f - b1t), vh = v / (1.f - b2t);
+    float p = master[i] - lr * mh / (sqrtf(vh) + eps);
+    master[i] = p;
+    w[i] = __float2half_rn(p);
+  }
+}
+
+// Register-resident inference.  Lane j of every warp holds hidden unit j's
+// weights (W1[:,j], b1[j], W2[:,j], b2[j], W3[j,:]) in registers for the whole
+// launch; a row's first layer is per lane, the second gathers the 32 first-layer
+// activations by shuffles, the output layer is a warp sum.  With `table` set the
+// rows are a graph's bucket features and the argmin kind of every populated
+// bucket is written to table[row]; otherwise the outputs go to y.
+__global__ void __launch_bounds__(256) k_model_infer(const __half *__restrict__ w, const float *__restrict__ x,
+                                                     uint32_t k, float *__restrict__ y,
+                                                     const unsigned long long *__restrict__ edges,
+                                                     uint8_t *__restrict__ table) {
+  const int lane = threadIdx.x & 31;
+  float w1[IN], w2[H], w3[OUT], b3[OUT];
+#pragma unroll
+  for (int f = 0; f < IN; f++) w1[f] = __half2float(w[O_W1 + f * H + lane]);
+  const float b1 = __half2float(w[O_B1 + lane]);
+#pragma unroll
+  for (int i = 0; i < H; i++) w2[i] = __half2float(w[O_W2 + i * H + lane]);
+  const float b2 = __half2float(w[O_B2 + lane]);
+#pragma unroll
+  for (int o = 0; o < OUT; o++) {
+    w3[o] = __half2float(w[O_W3 + lane * OUT + o]);
+    b3[o] = __half2float(w[O_B3 + o]);
+  }
+  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < k; r += warps) {
+    float a = b1;
+#pragma unroll
+    for (int f = 0; f < IN; f++) a = fmaf(x[(size_t)r * IN + f], w1[f], a);
+    const float h1 = a > 0.f ? a : 0.f;
+    float a2 = b2;
+#pragma unroll
+    for (int i = 0; i < H; i++) a2 = fmaf(__shfl_sync(ACCX_FULL_MASK, h1, i), w2[i], a2);
+    const float h2 = a2 > 0.f ? a2 : 0.f;
+    float out[OUT];
+#pragma unroll
+    for (int o = 0; o < OUT; o++) {
+      float p = h2 * w3[o];
+#pragma unroll
+      for (int d = 16; d >= 1; d >>= 1) p += __shfl_xor_sync(ACCX_FULL_MASK, p, d);
+      out[o] = p + b3[o];
+    }
+    if (lane == 0) {
+      if (table) {
+        int best = 0;
+#pragma unroll
+        for (int o = 1; o < OUT; o++)
+          if (out[o] < out[best]) best = o;
+        table[r] = (edges && edges[r] == 0) ? (uint8_t)ACCX_KIND_MERGE : (uint8_t)best;
+      } else {
+#pragma unroll
+        for (int o = 0; o < OUT; o++) y[(size_t)r * OUT + o] = out[o];
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Bucket statistics over owned edges: per block shared histograms, then global.
+#define NBB (ACCX_NB * ACCX_NB)
+template <int TILE>
+__global__ void __launch_bounds__(TILE) k_bucket_stats(const uint32_t *__restrict__ off, const int32_t *__restrict__ dst,
+                                                       uint32_t n, uint32_t m, unsigned long long *__restrict__ st) {
+  __shared__ accx_tile_rows<TILE> sh;
+  __shared__ unsigned long long hs[3 * NBB];
+  for (int i = threadIdx.x; i < 3 * NBB; i += TILE) hs[i] = 0;
+  uint32_t base = blockIdx.x * (uint32_t)TILE;
+  uint32_t e = base + threadIdx.x;
+  uint32_t u = accx_tile_row<TILE>(off, n, m, base, e, &sh);  // contains __syncthreads
+  if (e < m) {
+    uint32_t v = (uint32_t)dst[e];
+    uint32_t du = off[u + 1] - off[u], dv = off[v + 1] - off[v];
+    if (accx_owns(u, du, v, dv)) {
+      int b = accx_bucket(du) * ACCX_NB + accx_bucket(dv);
+      atomicAdd(&hs[b], 1ull);
+      atomicAdd(&hs[NBB + b], (unsigned long long)du);
+      atomicAdd(&hs[2 * NBB + b], (unsigned long long)dv);
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 3 * NBB; i += TILE)
+    if (hs[i]) atomicAdd(&st[i], hs[i]);
+}
+
+__device__ __forceinline__ void accx_feature_row(const unsigned long long *st, int b, uint32_t n, uint64_t m,
+                                                 float *x) {
+  const double E = (double)st[b];
+  for (int f = 0; f < IN; f++) x[f] = 0.f;
+  if (E <= 0) return;
+  const double mo = (double)st[NBB + b] / E, mp = (double)st[2 * NBB + b] / E;
+  const double lo = log2(mo), lp = log2(mp);
+  x[0] = (float)(lo / 16.0);
+  x[1] = (float)(lp / 16.0);
+  x[2] = (float)((lo - lp) / 16.0);
+  x[3] = (float)(log2(E + 1.0) / 32.0);
+  x[4] = (float)(log2((double)n + 1.0) / 32.0);
+  x[5] = (float)(log2((double)m + 1.0) / 32.0);
+  x[6] = (float)(lo * lp / 256.0);
+  x[7] = (float)(log2(E * mp + 1.0) / 40.0);
+}
+
+__global__ void k_features(const unsigned long long *__restrict__ st, uint32_t n, uint64_t m, float *__restrict__ x) {
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < NBB; b += gridDim.x * blockDim.x)
+    accx_feature_row(st, b, n, m, x + (size_t)b * IN);
+}
+
+// Per-handle cache: bucket statistics and features of the graph (it never
+// changes), plus the attached model.
+struct accx_graph_model_state {
+  unsigned long long *d_stats = nullptr;  // 3 * NBB
+  float *d_feat = nullptr;                // NBB * IN
+  bool ready = false;
+  accx_model *model = nullptr;
+};
+
+static accx_graph_model_state *state_of(accx_graph *g) {
+  if (!g->model) g->model = new (std::nothrow) accx_graph_model_state();
+  return static_cast<accx_graph_model_state *>(g->model);
+}
+
+void accx_model_release(accx_graph *g) {
+  auto *st = static_cast<accx_graph_model_state *>(g->model);
+  if (st) {
+    if (st->d_stats) cudaFree(st->d_stats);
+    if (st->d_feat) cudaFree(st->d_feat);
+    delete st;
+  }
+  g->model = nullptr;
+}
+
+static int ensure_features(accx_graph *g, cudaStream_t s) {
+  accx_graph_model_state *st = state_of(g);
+  if (!st) return ACCX_ERR_OOM;
+  if (st->ready) return ACCX_OK;
+  if (!st->d_stats) ACCX_CUDA_TRY(cudaMalloc(&st->d_stats, sizeof(unsigned long long) * 3 * NBB));
+  if (!st->d_feat) ACCX_CUDA_TRY(cudaMalloc(&st->d_feat, sizeof(float) * NBB * IN));
+  ACCX_CUDA_TRY(cudaMemsetAsync(st->d_stats, 0, sizeof(unsigned long long) * 3 * NBB, s));
+  const uint32_t m = (uint32_t)g->m;
+  if (m) k_bucket_stats<256><<<(m + 255) / 256, 256, 0, s>>>(g->d_off, g->d_dst, g->n, m, st->d_stats);
+  k_features<<<(NBB + 127) / 128, 128, 0, s>>>(st->d_stats, g->n, g->m, st->d_feat);
+  ACCX_CUDA_TRY(cudaGetLastError());
+  st->ready = true;
+  return ACCX_OK;
+}
+
+// The handle's ACCX_POLICY_MODEL table, computed on the device into g->d_table.
+int accx_model_table_device(accx_graph *g, cudaStream_t s) {
+  accx_graph_model_state *st = state_of(g);
+  if (!st || !st->model) return ACCX_ERR_NOT_READY;
+  int rc = ensure_features(g, s);
+  if (rc) return rc;
+  k_model_infer<<<8, 256, 0, s>>>(st->model->d_w, st->d_feat, NBB, nullptr, st->d_stats, g->d_table);
+  ACCX_CUDA_TRY(cudaGetLastError());
+  return ACCX_OK;
+}
 
 int accx_model_table(accx_graph *g, uint8_t *table) {
   (void)g;
@@ -9,4 +296,201 @@ int accx_model_table(accx_graph *g, uint8_t *table) {
   return ACCX_ERR_NOT_READY;
 }
 
-void accx_model_release(accx_graph *g) { g->model = nullptr; }
+// ---------------------------------------------------------------------------
+extern "C" int accx_model_create(uint64_t seed, accx_model **out) {
+  if (!out) return ACCX_ERR_INVALID_ARG;
+  *out = nullptr;
+  accx_model *m = new (std::nothrow) accx_model();
+  if (!m) return ACCX_ERR_OOM;
+  cudaGetDevice(&m->device);
+  if (cudaMalloc(&m->d_master, sizeof(float) * NP) != cudaSuccess || cudaMalloc(&m->d_w, sizeof(__half) * NP) != cudaSuccess ||
+      cudaMalloc(&m->d_m, sizeof(float) * NP) != cudaSuccess || cudaMalloc(&m->d_v, sizeof(float) * NP) != cudaSuccess ||
+      cudaMalloc(&m->d_grad, sizeof(float) * NP) != cudaSuccess || cudaMalloc(&m->d_loss, sizeof(float)) != cudaSuccess) {
+    cudaGetLastError();
+    accx_model_free(m);
+    return ACCX_ERR_OOM;
+  }
+  // He-style initialisation from a counter-based stream; output bias starts at
+  // -27 (about 7 ns per edge) so early predictions are in range.
+  std::vector<float> p(NP, 0.f);
+  uint64_t sm = seed * 0x9E3779B97F4A7C15ull + 12345;
+  auto unif = [&]() {
+    sm += 0x9E3779B97F4A7C15ull;
+    uint64_t z = sm;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
+  };
+  for (int i = 0; i < IN * H; i++) p[O_W1 + i] = (float)(unif() * sqrt(6.0 / IN));
+  for (int i = 0; i < H * H; i++) p[O_W2 + i] = (float)(unif() * sqrt(6.0 / H));
+  for (int i = 0; i < H * OUT; i++) p[O_W3 + i] = (float)(unif() * sqrt(6.0 / H) * 0.1);
+  for (int o = 0; o < OUT; o++) p[O_B3 + o] = -27.f;
+  int rc = accx_model_set_params(m, p.data());
+  if (rc) {
+    accx_model_free(m);
+    return rc;
+  }
+  *out = m;
+  return ACCX_OK;
+}
+
+extern "C" int accx_model_free(accx_model *m) {
+  if (!m) return ACCX_ERR_INVALID_ARG;
+  for (void *p : {(void *)m->d_master, (void *)m->d_w, (void *)m->d_m, (void *)m->d_v, (void *)m->d_grad,
+                  (void *)m->d_loss})
+    if (p) cudaFree(p);
+  delete m;
+  return ACCX_OK;
+}
+
+extern "C" int accx_model_set_params(accx_model *m, const float *params) {
+  if (!m || !params) return ACCX_ERR_INVALID_ARG;
+  ACCX_CUDA_TRY(cudaMemcpy(m->d_master, params, sizeof(float) * NP, cudaMemcpyHostToDevice));
+  k_to_half<<<4, 256>>>(m->d_master, m->d_w, NP);
+  ACCX_CUDA_TRY(cudaMemset(m->d_m, 0, sizeof(float) * NP));
+  ACCX_CUDA_TRY(cudaMemset(m->d_v, 0, sizeof(float) * NP));
+  ACCX_CUDA_TRY(cudaDeviceSynchronize());
+  m->step = 0;
+  return ACCX_OK;
+}
+
+extern "C" int accx_model_get_params(const accx_model *m, float *params) {
+  if (!m || !params) return ACCX_ERR_INVALID_ARG;
+  std::vector<__half> h(NP);
+  ACCX_CUDA_TRY(cudaMemcpy(h.data(), m->d_w, sizeof(__half) * NP, cudaMemcpyDeviceToHost));
+  for (int i = 0; i < NP; i++) params[i] = __half2float(h[i]);
+  return ACCX_OK;
+}
+
+struct dev_samples {
+  float *x = nullptr, *t = nullptr;
+  int32_t *k = nullptr;
+  ~dev_samples() {
+    if (x) cudaFree(x);
+    if (t) cudaFree(t);
+    if (k) cudaFree(k);
+  }
+};
+
+static int upload_samples(dev_samples &d, const float *x, const int32_t *kind, const float *target, uint32_t k) {
+  for (uint32_t i = 0; i < k; i++)
+    if (kind[i] < 0 || kind[i] >= OUT) return ACCX_ERR_INVALID_ARG;
+  ACCX_CUDA_TRY(cudaMalloc(&d.x, sizeof(float) * (size_t)k * IN));
+  ACCX_CUDA_TRY(cudaMalloc(&d.t, sizeof(float) * k));
+  ACCX_CUDA_TRY(cudaMalloc(&d.k, sizeof(int32_t) * k));
+  ACCX_CUDA_TRY(cudaMemcpy(d.x, x, sizeof(float) * (size_t)k * IN, cudaMemcpyHostToDevice));
+  ACCX_CUDA_TRY(cudaMemcpy(d.t, target, sizeof(float) * k, cudaMemcpyHostToDevice));
+  ACCX_CUDA_TRY(cudaMemcpy(d.k, kind, sizeof(int32_t) * k, cudaMemcpyHostToDevice));
+  return ACCX_OK;
+}
+
+static int grad_pass(accx_model *m, const dev_samples &d, uint32_t k) {
+  ACCX_CUDA_TRY(cudaMemsetAsync(m->d_grad, 0, sizeof(float) * NP));
+  ACCX_CUDA_TRY(cudaMemsetAsync(m->d_loss, 0, sizeof(float)));
+  int blocks = (int)((k + 127) / 128);
+  if (blocks > 64) blocks = 64;
+  k_model_grad<<<blocks, 128>>>(m->d_w, d.x, d.k, d.t, k, m->d_grad, m->d_loss);
+  ACCX_CUDA_TRY(cudaGetLastError());
+  return ACCX_OK;
+}
+
+extern "C" int accx_model_loss_grad(accx_model *m, const float *x, const int32_t *kind, const float *target,
+                                    uint32_t k, float *grad, float *loss) {
+  if (!m || !x || !kind || !target || !k) return ACCX_ERR_INVALID_ARG;
+  dev_samples d;
+  int rc = upload_samples(d, x, kind, target, k);
+  if (!rc) rc = grad_pass(m, d, k);
+  if (rc) return rc;
+  if (grad) ACCX_CUDA_TRY(cudaMemcpy(grad, m->d_grad, sizeof(float) * NP, cudaMemcpyDeviceToHost));
+  if (loss) ACCX_CUDA_TRY(cudaMemcpy(loss, m->d_loss, sizeof(float), cudaMemcpyDeviceToHost));
+  return ACCX_OK;
+}
+
+extern "C" int accx_model_train(accx_model *m, const float *x, const int32_t *kind, const float *target, uint32_t k,
+                                int epochs, float lr, float *final_loss) {
+  if (!m || !x || !kind || !target || !k || epochs < 1 || !(lr > 0)) return ACCX_ERR_INVALID_ARG;
+  dev_samples d;
+  int rc = upload_samples(d, x, kind, target, k);
+  if (rc) return rc;
+  for (int ep = 0; ep < epochs; ep++) {
+    rc = grad_pass(m, d, k);
+    if (rc) return rc;
+    m->step++;
+    const float b1t = powf(0.9f, (float)m->step), b2t = powf(0.999f, (float)m->step);
+    k_model_adam<<<(NP + 255) / 256, 256>>>(m->d_master, m->d_w, m->d_m, m->d_v, m->d_grad, lr, b1t, b2t);
+  }
+  rc = grad_pass(m, d, k);
+  if (rc) return rc;
+  float l = 0;
+  ACCX_CUDA_TRY(cudaMemcpy(&l, m->d_loss, sizeof(float), cudaMemcpyDeviceToHost));
+  if (final_loss) *final_loss = l;
+  return ACCX_OK;
+}
+
+extern "C" int accx_model_predict(accx_model *m, const float *x, uint32_t k, float *y) {
+  if (!m || !x || !y || !k) return ACCX_ERR_INVALID_ARG;
+  float *dx = nullptr, *dy = nullptr;
+  ACCX_CUDA_TRY(cudaMalloc(&dx, sizeof(float) * (size_t)k * IN));
+  cudaError_t e = cudaMalloc(&dy, sizeof(float) * (size_t)k * OUT);
+  if (e == cudaSuccess) e = cudaMemcpy(dx, x, sizeof(float) * (size_t)k * IN, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    k_model_infer<<<8, 256>>>(m->d_w, dx, k, dy, nullptr, nullptr);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(y, dy, sizeof(float) * (size_t)k * OUT, cudaMemcpyDeviceToHost);
+  cudaFree(dx);
+  if (dy) cudaFree(dy);
+  if (e != cudaSuccess) {
+    accx_set_cuda_error(e, "model_predict", __FILE__, __LINE__);
+    return ACCX_ERR_CUDA;
+  }
+  return ACCX_OK;
+}
+
+extern "C" int accx_bucket_stats(accx_graph *g, uint64_t *edges, double *sum_owner, double *sum_other) {
+  if (!g) return ACCX_ERR_INVALID_ARG;
+  int rc = ensure_features(g, nullptr);
+  if (rc) return rc;
+  std::vector<unsigned long long> h(3 * NBB);
+  ACCX_CUDA_TRY(cudaMemcpy(h.data(), state_of(g)->d_stats, sizeof(unsigned long long) * 3 * NBB, cudaMemcpyDeviceToHost));
+  for (int b = 0; b < NBB; b++) {
+    if (edges) edges[b] = h[b];
+    if (sum_owner) sum_owner[b] = (double)h[NBB + b];
+    if (sum_other) sum_other[b] = (double)h[2 * NBB + b];
+  }
+  return ACCX_OK;
+}
+
+extern "C" int accx_bucket_features(accx_graph *g, float *features) {
+  if (!g || !features) return ACCX_ERR_INVALID_ARG;
+  int rc = ensure_features(g, nullptr);
+  if (rc) return rc;
+  ACCX_CUDA_TRY(cudaMemcpy(features, state_of(g)->d_feat, sizeof(float) * NBB * IN, cudaMemcpyDeviceToHost));
+  return ACCX_OK;
+}
+
+extern "C" int accx_model_table_for(accx_model *m, accx_graph *g, uint8_t *table) {
+  if (!m || !g || !table) return ACCX_ERR_INVALID_ARG;
+  int rc = ensure_features(g, nullptr);
+  if (rc) return rc;
+  uint8_t *dt = nullptr;
+  ACCX_CUDA_TRY(cudaMalloc(&dt, NBB));
+  k_model_infer<<<8, 256>>>(m->d_w, state_of(g)->d_feat, NBB, nullptr, state_of(g)->d_stats, dt);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpy(table, dt, NBB, cudaMemcpyDeviceToHost);
+  cudaFree(dt);
+  if (e != cudaSuccess) {
+    accx_set_cuda_error(e, "model_table_for", __FILE__, __LINE__);
+    return ACCX_ERR_CUDA;
+  }
+  return ACCX_OK;
+}
+
+extern "C" int accx_graph_set_model(accx_graph *g, accx_model *m) {
+  if (!g) return ACCX_ERR_INVALID_ARG;
+  accx_graph_model_state *st = state_of(g);
+  if (!st) return ACCX_ERR_OOM;
+  st->model = m;
+  return ACCX_OK;
+}

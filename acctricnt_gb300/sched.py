@@ -1,0 +1,166 @@
+"""Learned kernel scheduler: training data, training, tables and regret.
+
+The cost model (accx_model, csrc/model.cu) predicts, per degree bucket and per
+kernel kind (merge, gallop, bitmap), the log2 time per owned edge.  Training
+data are timings the counting kernels themselves produce: for every populated
+bucket and every kind, one count runs with only that bucket enabled (all other
+buckets set to ACCX_KIND_SKIP) and the library's CUDA events time the counting
+phases.  The same exhaustive per-bucket timing, run on a graph the model has
+not seen, is the judge of the model's regret: the time its per-bucket choice
+costs above the best choice per bucket.
+
+The reference has no counterpart: it fixes the choice by a degree ratio of 50
+(scan_xp_multi_gpu_multi_pass_common.cu:57-59, :105-117), the heuristic policy
+here.
+"""
+import json
+import os
+import time
+
+import numpy as np
+
+from . import BUILD_DIR
+from . import accx
+
+NB = accx.NB
+KINDS = accx.KIND_NAMES
+MODEL_PATH = os.path.join(BUILD_DIR, "sched_model.json")
+
+
+def _count_phase_ms(G, table, reps, stream=None):
+    best = None
+    for _ in range(reps):
+        G.count(policy="table", table=table, out=None, timing=True, stream=stream)
+        ph = G.timings()
+        t = ph["merge"] + ph["gallop"] + ph["bitmap"]
+        best = t if best is None else min(best, t)
+    return best
+
+
+def bucket_timings(G, reps=2, min_edges=1, stream=None):
+    """Exhaustive per-bucket timing.  Returns (edges[NB*NB], ms[NB*NB, 3]) with
+    NaN for buckets without owned edges."""
+    edges, _, _ = G.bucket_stats()
+    skip = np.full(NB * NB, accx.KIND_SKIP, np.uint8)
+    G.count(policy="table", table=skip, out=None, stream=stream)  # warm
+    base = _count_phase_ms(G, skip, max(reps, 3), stream)
+    T = np.full((NB * NB, 3), np.nan)
+    for b in np.nonzero(edges >= min_edges)[0]:
+        for k in range(3):
+            t = skip.copy()
+            t[b] = k
+            T[b, k] = max(_count_phase_ms(G, t, reps, stream) - base, 1e-4)
+    return edges, T
+
+
+def samples(G, edges, T, min_edges=32):
+    """Training rows: (features, kind, log2 seconds per edge)."""
+    X = G.bucket_features()
+    xs, ks, ys = [], [], []
+    for b in np.nonzero(edges >= min_edges)[0]:
+        for k in range(3):
+            if np.isfinite(T[b, k]):
+                xs.append(X[b])
+                ks.append(k)
+                ys.append(np.log2(T[b, k] * 1e-3 / float(edges[b])))
+    return np.array(xs, np.float32).reshape(-1, accx.MODEL_IN), np.array(ks, np.int32), np.array(ys, np.float32)
+
+
+def exhaustive_table(edges, T):
+    """Best kind per bucket by measurement (merge where nothing was measured)."""
+    t = np.zeros(NB * NB, np.uint8)
+    ok = np.isfinite(T).all(1)
+    t[ok] = np.argmin(T[ok], 1)
+    return t.reshape(NB, NB)
+
+
+def heuristic_table(edges, sum_owner, sum_other):
+    """The reference's fixed rule at bucket level: galloping when the mean
+    owner degree exceeds 50 x the mean other degree, else merge."""
+    t = np.zeros(NB * NB, np.uint8)
+    nz = edges > 0
+    mo = np.where(nz, sum_owner / np.maximum(edges, 1), 0)
+    mp = np.where(nz, sum_other / np.maximum(edges, 1), 1)
+    t[nz & (50 * mp < mo)] = accx.KIND_GALLOP
+    return t.reshape(NB, NB)
+
+
+def table_time(table, T):
+    """Sum of measured per-bucket times (ms) of a table's choices."""
+    tab = np.asarray(table).reshape(-1)
+    ok = np.isfinite(T).all(1)
+    return float(T[np.nonzero(ok)[0], tab[ok]].sum())
+
+
+def regret(table, edges, T):
+    best = table_time(exhaustive_table(edges, T), T)
+    got = table_time(table, T)
+    return {"chosen_ms": got, "best_ms": best, "regret_ms": got - best, "regret_frac": (got - best) / best if best else 0}
+
+
+def training_graphs():
+    return [accx.rmat_params(16, 16, seed=11), accx.rmat_params(17, 16, seed=12), accx.rmat_params(18, 16, seed=13),
+            accx.rmat_params(19, 8, seed=14), accx.er_params(1 << 17, 24, seed=15),
+            accx.chung_lu_params(1 << 18, 24, 2.1, 20000, seed=16), accx.chung_lu_params(1 << 17, 12, 2.5, 5000, seed=17)]
+
+
+def collect(graph_params, reps=2, relabel=True, log=None):
+    xs, ks, ys = [], [], []
+    for p in graph_params:
+        t0 = time.perf_counter()
+        G = accx.Graph.generate(p)
+        if relabel:
+            G.relabel()
+        edges, T = bucket_timings(G, reps=reps)
+        x, k, y = samples(G, edges, T)
+        xs.append(x)
+        ks.append(k)
+        ys.append(y)
+        if log:
+            log("collected %d rows from n=%d m=%d in %.1f s" % (len(k), G.n, G.m, time.perf_counter() - t0))
+        G.free()
+    return np.concatenate(xs), np.concatenate(ks), np.concatenate(ys)
+
+
+def train_default(seed=1, epochs=4000, lr=3e-3, log=None):
+    t0 = time.perf_counter()
+    x, k, y = collect(training_graphs(), log=log)
+    tc = time.perf_counter() - t0
+    model = accx.Model(seed)
+    loss0, _ = model.loss_grad(x, k, y)
+    t1 = time.perf_counter()
+    loss = model.train(x, k, y, epochs=epochs, lr=lr)
+    info = {"rows": int(len(k)), "collect_s": round(tc, 2), "train_s": round(time.perf_counter() - t1, 2),
+            "epochs": epochs, "loss_initial": loss0, "loss_final": loss}
+    return model, info
+
+
+def save(model, info, path=MODEL_PATH):
+    with open(path, "w") as f:
+        json.dump({"params": model.params().tolist(), "info": info}, f)
+
+
+def load(path=MODEL_PATH):
+    with open(path) as f:
+        d = json.load(f)
+    m = accx.Model(1)
+    m.set_params(np.array(d["params"], np.float32))
+    return m, d["info"]
+
+
+def default_model(retrain=False, log=None):
+    if not retrain and os.path.exists(MODEL_PATH):
+        try:
+            return load()
+        except Exception:
+            pass
+    model, info = train_default(log=log)
+    save(model, info)
+    return model, info
+
+
+def schedule_for(G, model=None, info=None):
+    """(table[NB][NB], info) chosen by the cost model for graph G."""
+    if model is None:
+        model, info = default_model()
+    return model.table_for(G), dict(info or {})

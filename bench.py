@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-regret", dest="regret", action="store_false",
+                    help="skip the exhaustive per-bucket timing that measures the scheduler's regret")
     return ap.parse_args()
 
 
@@ -146,16 +148,19 @@ class ClockSampler:
 
 
 def pick_policy(G, args):
-    """The scheduled policy: the trained cost model when available, else the
-    fixed policy given on the command line."""
+    """The scheduled policy: the cost model (trained on the GPU from per-bucket
+    kernel timings of small training graphs, cached in the build folder) attached
+    to the graph, so every count runs the register-resident inference kernel and
+    classifies with its table on the device."""
     if args.policy != "auto":
-        return args.policy, None
-    try:
-        from acctricnt_gb300 import sched
-        table, info = sched.schedule_for(G)
-        return "table", (table, info)
-    except Exception as e:  # no model yet: report the best fixed policy instead
-        return "bitmap", {"note": "cost model unavailable: %s" % e}
+        return args.policy, None, {}
+    from acctricnt_gb300 import sched
+    t0 = time.perf_counter()
+    model, info = sched.default_model()
+    info = dict(info)
+    info["model_ready_s"] = round(time.perf_counter() - t0, 2)
+    G.set_model(model)
+    return "model", model, info
 
 
 def time_counts(G, policy, table, steps, warmup, tstream, world, timing=True):
@@ -199,7 +204,7 @@ def measure_queries(G, reps):
             "eps": list(QUERY_EPS), "mu": QUERY_MU}
 
 
-def measure_e2e(G, policy, table, reps):
+def measure_e2e(G, policy, table, reps, model=None):
     """Through the C ABI with host buffers: pinned host CSR -> accx_graph_create
     (copy + validation) -> count -> counts copied back to pinned host memory."""
     import torch
@@ -213,6 +218,9 @@ def measure_e2e(G, policy, table, reps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         H = accx.Graph.from_device(t_off.data_ptr(), t_dst.data_ptr(), G.n, G.m, validate=True)
+        H.relabel()
+        if model is not None:
+            H.set_model(model)
         H.count(policy=policy, table=table, out=t_cnt.data_ptr())
         H.free()
         dt = time.perf_counter() - t0
@@ -221,7 +229,8 @@ def measure_e2e(G, policy, table, reps):
     t = statistics.median(times)
     return {"value": round(G.m / t / 1e9, 4), "unit": UNIT, "h2d_bytes_per_step": 4 * (G.n + 1) + 4 * G.m,
             "d2h_bytes_per_step": 4 * G.m, "ms_per_step": round(t * 1e3, 3),
-            "path": "accx_graph_create(host pinned CSR, validate) + accx_cn_count(host pinned out)"}
+            "path": "accx_graph_create(host pinned CSR, validate) + accx_graph_relabel + accx_cn_count(model policy, "
+                    "host pinned out)"}
 
 
 def cpu_baseline(off, dst, budget_s, nthreads):
@@ -252,7 +261,7 @@ def alg_bytes(G, dominant, stats, owner_work):
     if dominant == "merge":
         return 4 * stats["merge"]["work"] + 4 * owner_work["merge"] + 12 * stats["merge"]["edges"]
     if dominant == "gallop":
-        return 4 * stats["gallop"]["work"] + 12 * stats["gallop"]["edges"]
+        return 4 * stats["gallop"]["work"] + 16 * stats["gallop"]["edges"]
     if dominant == "mirror":
         return 4 * 4 * G.m
     return 8 * G.m
@@ -265,8 +274,12 @@ def run_gb300(args):
     G = accx.Graph.generate(accx.rmat_params(args.scale, args.edge_factor, seed=1 + rank))
     stream = torch.cuda.Stream()
     sp = stream.cuda_stream
-    policy, sched_info = pick_policy(G, args)
-    table = sched_info[0] if isinstance(sched_info, tuple) else None
+    t0 = time.perf_counter()
+    G.relabel(stream=sp)
+    torch.cuda.synchronize()
+    relabel_ms = (time.perf_counter() - t0) * 1e3
+    policy, model, sched_info = pick_policy(G, args)
+    table = None
     # correctness guard: the scheduled and plain counts are identical
     G.count(policy=policy, table=table, out=None, stream=sp)
     a = G.count(policy=policy, table=table, stream=sp)
@@ -280,6 +293,19 @@ def run_gb300(args):
     owner_work = G.owner_work()
     plain_ms, plain_phases = time_counts(G, "heuristic", None, args.steps, args.warmup, stream, world)
     plain_ms = max_over_ranks(plain_ms, world)
+    bm_ms, _ = time_counts(G, "bitmap", None, max(1, args.steps // 2), 1, stream, world)
+    if model is not None and args.regret and rank == 0:
+        from acctricnt_gb300 import sched
+        t0 = time.perf_counter()
+        edges, T = sched.bucket_timings(G, reps=1, stream=sp)
+        e, so, sp_ = G.bucket_stats()
+        mt = model.table_for(G)
+        r = sched.regret(mt, edges, T)
+        sched_info.update({"regret": {k: round(v, 4) for k, v in r.items()},
+                           "heuristic_bucket_sum_ms": round(sched.table_time(sched.heuristic_table(e, so, sp_), T), 3),
+                           "bitmap_bucket_sum_ms": round(sched.table_time(np.full((24, 24), 2), T), 3),
+                           "exhaustive_timing_s": round(time.perf_counter() - t0, 2),
+                           "kinds_chosen": {k: int((mt.reshape(-1)[e > 0] == i).sum()) for i, k in enumerate(accx.KIND_NAMES)}})
     total_m = sum_over_ranks(G.m, world)
     value = total_m / (ms / 1e3) / 1e9
     plain_value = total_m / (plain_ms / 1e3) / 1e9
@@ -309,7 +335,7 @@ def run_gb300(args):
                 "merge_equiv_bytes": int(4 * float(np.sum(np.diff(G.download()[0]).astype(np.float64) ** 2)) + 4 * G.m)}
     e2e = None
     if not args.no_e2e and rank == 0:
-        e2e = measure_e2e(G, policy, table, 2)
+        e2e = measure_e2e(G, policy, table, 2, model)
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
         off, dst = G.download()
@@ -325,10 +351,12 @@ def run_gb300(args):
             "plain": {"policy": "heuristic", "value": round(plain_value, 4), "ms_per_step": round(plain_ms, 3),
                       "phases_ms": {k: round(v, 3) for k, v in plain_phases.items()}},
             "speedup_vs_plain": round(plain_ms / ms, 3), "bit_exact_vs_plain": bit_exact,
+            "bitmap_all": {"ms_per_step": round(bm_ms, 3), "value": round(total_m / (bm_ms / 1e3) / 1e9, 4)},
+            "relabel_ms": round(relabel_ms, 2),
             "phases_ms": {k: round(v, 3) for k, v in phases.items()}, "kinds": stats,
             "scan": scan, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-            "gpu_launches": 6 * args.steps, "clocks": clk.summary(),
-            "sched": sched_info[1] if isinstance(sched_info, tuple) else sched_info}
+            "gpu_launches": (8 if policy == "model" else 7) * args.steps, "clocks": clk.summary(),
+            "sched": sched_info}
     if rank == 0:
         print(json.dumps(line), flush=True)
 

@@ -118,6 +118,7 @@ int accx_write_graph_dir(const char *dir, const uint32_t *off, const int32_t *ds
 #define ACCX_KIND_GALLOP 1  /* per-element binary search of the small list in the large one */
 #define ACCX_KIND_BITMAP 2  /* per-owner shared-memory bitmap over id windows, ballot/popc probe */
 #define ACCX_NUM_KINDS 3
+#define ACCX_KIND_SKIP 3    /* table only: leave the bucket uncounted (per-bucket timing runs) */
 
 /* Policies. */
 #define ACCX_POLICY_HEURISTIC 0 /* reference rule: gallop iff d_max/50 > d_min, else merge */
@@ -182,6 +183,45 @@ int accx_cn_last_timings(const accx_graph *g, float ms[ACCX_NUM_PHASES]);
 int accx_cn_count_noalloc(const uint32_t *off, const int32_t *dst, uint32_t n, uint64_t m, int32_t bias,
                           int32_t *cnt, void *stream);
 uint64_t accx_cn_count_noalloc_max_entries(void);
+
+/* ---- learned scheduler: an MLP cost model per degree bucket ------------------
+ * No counterpart in the reference, which fixes the kernel choice by a degree
+ * ratio (scan_xp_multi_gpu_multi_pass_common.cu:57-59, :105-117).  The model maps
+ * a bucket's features (owner/other mean degree, their ratio, bucket size, graph
+ * size; ACCX_MODEL_IN floats) to the predicted log2 time per edge of each kernel
+ * kind; the scheduler picks the cheapest kind per bucket.  Weights are FP16,
+ * accumulation FP32; training, inference and the gradient run as the library's
+ * own CUDA kernels. */
+#define ACCX_MODEL_IN 8
+#define ACCX_MODEL_H 32
+#define ACCX_MODEL_OUT ACCX_NUM_KINDS
+#define ACCX_MODEL_NPARAMS (ACCX_MODEL_IN * ACCX_MODEL_H + ACCX_MODEL_H + ACCX_MODEL_H * ACCX_MODEL_H + ACCX_MODEL_H + \
+                            ACCX_MODEL_H * ACCX_MODEL_OUT + ACCX_MODEL_OUT)
+typedef struct accx_model accx_model;
+
+int accx_model_create(uint64_t seed, accx_model **out);
+int accx_model_free(accx_model *m);
+/* Parameters as FP32 (the FP16 weights widened); set rounds them to FP16. */
+int accx_model_get_params(const accx_model *m, float *params);
+int accx_model_set_params(accx_model *m, const float *params);
+/* Per-bucket statistics of a graph's owned edges: edges[b], and the sums of the
+ * owner's and the other endpoint's degree, b = owner_bucket*ACCX_NB + other_bucket. */
+int accx_bucket_stats(accx_graph *g, uint64_t *edges, double *sum_owner, double *sum_other);
+/* Feature rows (ACCX_MODEL_IN floats per bucket, ACCX_NB*ACCX_NB rows) of a graph. */
+int accx_bucket_features(accx_graph *g, float *features);
+/* Mean loss and its gradient (FP32, ACCX_MODEL_NPARAMS) over k samples:
+ * x[k*ACCX_MODEL_IN], kind[k], target[k] (log2 seconds per edge). */
+int accx_model_loss_grad(accx_model *m, const float *x, const int32_t *kind, const float *target, uint32_t k,
+                         float *grad, float *loss);
+/* Adam training on the GPU over the samples; returns the final mean loss. */
+int accx_model_train(accx_model *m, const float *x, const int32_t *kind, const float *target, uint32_t k,
+                     int epochs, float lr, float *final_loss);
+/* Predictions (log2 seconds per edge, ACCX_MODEL_OUT per row) for k feature rows. */
+int accx_model_predict(accx_model *m, const float *x, uint32_t k, float *y);
+/* The kind table the model picks for a graph (runs on the device). */
+int accx_model_table_for(accx_model *m, accx_graph *g, uint8_t *table);
+/* Attach a model to a graph handle for ACCX_POLICY_MODEL (the handle does not own it). */
+int accx_graph_set_model(accx_graph *g, accx_model *m);
 
 /* ---- SCAN query ------------------------------------------------------------- */
 #define ACCX_UNCLASSIFIED 0

@@ -76,6 +76,7 @@ def _load():
         "accx_write_graph_dir": (C.c_int, [C.c_char_p, P, P, C.c_uint32, C.c_uint64]),
         "accx_cn_count": (C.c_int, [P, C.POINTER(CountOpts), P, P]),
         "accx_cn_last_stats": (C.c_int, [P, P, P]),
+        "accx_cn_read": (C.c_int, [P, P, P]),
         "accx_cn_count_noalloc": (C.c_int, [P, P, C.c_uint32, C.c_uint64, C.c_int32, P, P]),
         "accx_cn_count_noalloc_max_entries": (C.c_uint64, []),
         "accx_cn_last_owner_work": (C.c_int, [P, P]),
@@ -96,6 +97,13 @@ def _load():
         "accx_model_predict": (C.c_int, [P, P, C.c_uint32, P]),
         "accx_model_table_for": (C.c_int, [P, P, P]),
         "accx_graph_set_model": (C.c_int, [P, P]),
+        "accx_batch_create": (C.c_int, [P, C.c_int, P, C.POINTER(P)]),
+        "accx_batch_free": (C.c_int, [P]),
+        "accx_batch_union": (P, [P]),
+        "accx_batch_graph_range": (C.c_int, [P, C.c_int, P, P, P, P]),
+        "accx_batch_capture": (C.c_int, [P, C.POINTER(CountOpts), P]),
+        "accx_batch_launch": (C.c_int, [P, P]),
+        "accx_autotune": (C.c_int, [P, C.POINTER(CountOpts), C.c_int, C.POINTER(CountOpts), P, P, P, P]),
         "accx_similar_exact_batch": (C.c_int, [C.c_uint64, P, P, P, C.c_double, P]),
     }
     for name, (res, args) in sigs.items():
@@ -246,9 +254,9 @@ class Graph:
         return bool(lib.accx_graph_is_relabeled(self._h))
 
     def free(self):
-        if self._h:
+        if self._h and not getattr(self, "_owned_by_batch", False):
             lib.accx_graph_free(self._h)
-            self._h = None
+        self._h = None
 
     def __del__(self):
         try:
@@ -294,6 +302,12 @@ class Graph:
         del keep
         return None
 
+    def read_counts(self, stream=None):
+        """The resident counts (after a count or a captured replay), to the host."""
+        res = np.zeros(max(self.m, 1), np.int32)
+        _check(lib.accx_cn_read(self._h, _ptr(res), _stream_ptr(stream)), "cn_read")
+        return res[:self.m]
+
     def last_stats(self):
         e = np.zeros(3, np.uint64)
         w = np.zeros(3, np.uint64)
@@ -310,6 +324,18 @@ class Graph:
         ms = np.zeros(5, np.float32)
         _check(lib.accx_cn_last_timings(self._h, _ptr(ms)), "cn_last_timings")
         return dict(zip(PHASES, (float(x) for x in ms)))
+
+    def autotune(self, policy="bitmap", reps=2, stream=None):
+        """Fastest bitmap-kernel launch shape for `policy`; returns (kwargs, ms, all_ms)."""
+        base, keep = self._opts(policy, None, 0, 0, 0)
+        best = CountOpts()
+        bms = C.c_float()
+        allms = np.zeros(16, np.float32)
+        nc = C.c_int()
+        _check(lib.accx_autotune(self._h, C.byref(base), int(reps), C.byref(best), C.byref(bms), _ptr(allms),
+                                 C.byref(nc), _stream_ptr(stream)), "autotune")
+        return ({"block_warps": best.block_warps, "window_kb": best.bitmap_window_kb,
+                 "sparse_kb": best.sparse_table_kb}, float(bms.value), allms[:nc.value].tolist())
 
     def bucket_stats(self):
         e = np.zeros(NB * NB, np.uint64)
@@ -403,3 +429,54 @@ class Model:
         t = np.zeros(NB * NB, np.uint8)
         _check(lib.accx_model_table_for(self._h, graph._h, _ptr(t)), "model_table_for")
         return t.reshape(NB, NB)
+
+
+class Batch:
+    """K graphs joined into one disjoint-union CSR (accx_batch)."""
+
+    def __init__(self, graphs, stream=None):
+        self.graphs = list(graphs)
+        arr = (C.c_void_p * len(self.graphs))(*[g._h for g in self.graphs])
+        self._h = C.c_void_p()
+        _check(lib.accx_batch_create(arr, len(self.graphs), _stream_ptr(stream), C.byref(self._h)), "batch_create")
+        u = Graph.__new__(Graph)
+        u._h = C.c_void_p(lib.accx_batch_union(self._h))
+        n = C.c_uint32()
+        m = C.c_uint64()
+        _check(lib.accx_graph_size(u._h, C.byref(n), C.byref(m)), "graph_size")
+        u.n, u.m = int(n.value), int(m.value)
+        u._owned_by_batch = True
+        self.union = u
+        self.ranges = []
+        for i in range(len(self.graphs)):
+            vb, nn, eb, mm = C.c_uint32(), C.c_uint32(), C.c_uint64(), C.c_uint64()
+            _check(lib.accx_batch_graph_range(self._h, i, C.byref(vb), C.byref(nn), C.byref(eb), C.byref(mm)),
+                   "batch_graph_range")
+            self.ranges.append((int(vb.value), int(nn.value), int(eb.value), int(mm.value)))
+
+    def free(self):
+        if self._h:
+            self.union._h = None  # owned by the batch
+            lib.accx_batch_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def capture(self, policy="model", bias=0, stream=None, **kw):
+        opts, keep = Graph._opts(policy, None, bias, kw.get("block_warps", 0), kw.get("window_kb", 0), False,
+                                 kw.get("sparse_kb", 0))
+        _check(lib.accx_batch_capture(self._h, C.byref(opts), _stream_ptr(stream)), "batch_capture")
+
+    def launch(self, stream=None):
+        _check(lib.accx_batch_launch(self._h, _stream_ptr(stream)), "batch_launch")
+
+    def split(self, arr, per="entry"):
+        """Slices of a union-wide array per graph (per entry or per vertex)."""
+        out = []
+        for vb, n, eb, m in self.ranges:
+            out.append(arr[eb:eb + m] if per == "entry" else arr[vb:vb + n])
+        return out

@@ -691,3 +691,9 @@ extern "C" int accx_cn_last_timings(const accx_graph *g, float ms[ACCX_NUM_PHASE
   for (int i = 0; i < ACCX_NUM_PHASES; i++) ACCX_CUDA_TRY(cudaEventElapsedTime(&ms[i], g->ev[i], g->ev[i + 1]));
   return ACCX_OK;
 }
+
+extern "C" int accx_cn_read(const accx_graph *g, int32_t *out, void *stream) {
+  if (!g || (!out && g->m)) return ACCX_ERR_INVALID_ARG;
+  if (!g->cnt_valid || !g->d_cnt) return ACCX_ERR_NOT_READY;
+  return accx_copy_out(out, g->d_cnt, sizeof(int32_t) * (size_t)g->m, (cudaStream_t)stream);
+}

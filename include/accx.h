@@ -148,6 +148,10 @@ typedef struct {
  * or device).  opts NULL = heuristic policy, bias 0. */
 int accx_cn_count(accx_graph *g, const accx_count_opts *opts, int32_t *out, void *stream);
 
+/* Copies the resident counts of the last count (or captured replay) to `out`
+ * (host or device), without counting again. */
+int accx_cn_read(const accx_graph *g, int32_t *out, void *stream);
+
 /* Per-kind statistics of the last accx_cn_count: edges[k] owned edges and
  * work[k] probe elements assigned to kind k. */
 int accx_cn_last_stats(const accx_graph *g, uint64_t edges[ACCX_NUM_KINDS], uint64_t work[ACCX_NUM_KINDS]);
@@ -222,6 +226,34 @@ int accx_model_predict(accx_model *m, const float *x, uint32_t k, float *y);
 int accx_model_table_for(accx_model *m, accx_graph *g, uint8_t *table);
 /* Attach a model to a graph handle for ACCX_POLICY_MODEL (the handle does not own it). */
 int accx_graph_set_model(accx_graph *g, accx_model *m);
+
+/* ---- batches of uneven graphs -------------------------------------------------
+ * No reference counterpart (the reference counts one graph per process).  A
+ * batch joins K graphs into one disjoint-union CSR on the device; one count and
+ * one SCAN query over the union give each graph's results (graph i owns vertex
+ * ids [vbase_i, vbase_i + n_i) and entries [ebase_i, ebase_i + m_i); cluster ids
+ * are union ids).  The count is a fixed launch sequence of persistent kernels,
+ * recorded once into a CUDA graph by accx_batch_capture and replayed by
+ * accx_batch_launch. */
+typedef struct accx_batch accx_batch;
+int accx_batch_create(accx_graph *const *graphs, int k, void *stream, accx_batch **out);
+int accx_batch_free(accx_batch *b);
+/* The union graph (owned by the batch): count, relabel, query and download it
+ * with the accx_graph functions. */
+accx_graph *accx_batch_union(accx_batch *b);
+int accx_batch_graph_range(const accx_batch *b, int i, uint32_t *vbase, uint32_t *n, uint64_t *ebase, uint64_t *m);
+/* Records the count of the union (opts as for accx_cn_count, not ACCX_POLICY_TABLE
+ * and without timing) on `stream` (not the legacy default stream); runs it once
+ * eagerly first so every scratch array exists before capture. */
+int accx_batch_capture(accx_batch *b, const accx_count_opts *opts, void *stream);
+int accx_batch_launch(accx_batch *b, void *stream);
+
+/* Launch autotuner: times candidate shapes of the bitmap kernel (CTA warps,
+ * dense-window KiB, sparse-table KiB) for a policy on this graph and returns the
+ * fastest in *best (other fields copied from *base).  all_ms (optional, >= 8
+ * floats) receives each candidate's time, -1 for shapes the device cannot run. */
+int accx_autotune(accx_graph *g, const accx_count_opts *base, int reps, accx_count_opts *best, float *best_ms,
+                  float *all_ms, int *ncand, void *stream);
 
 /* ---- SCAN query ------------------------------------------------------------- */
 #define ACCX_UNCLASSIFIED 0

@@ -44,15 +44,49 @@ class GenParams(C.Structure):
 
 class CountOpts(C.Structure):
     _fields_ = [("policy", C.c_int), ("table", C.POINTER(C.c_uint8)), ("bias", C.c_int32),
-                ("block_warps", C.c_int), ("bitmap_window_kb", C.c_int), ("timing", C.c_int), ("sparse_table_kb", C.c_int)]
+                ("block_warps", C.c_int), ("bitmap_window_kb", C.c_int), ("timing", C.c_int), ("sparse_table_kb", C.c_int),
+                ("sm_limit", C.c_int)]
 
 
 class ScanSummary(C.Structure):
     _fields_ = [("cores", C.c_uint32), ("clusters", C.c_uint32), ("hubs", C.c_uint32), ("outliers", C.c_uint32),
-                ("similar_entries", C.c_uint64), ("noncore_pairs", C.c_uint64)]
+                ("similar_entries", C.c_uint64), ("noncore_pairs", C.c_uint64), ("digest", C.c_uint64)]
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
+REQ_QUERY, REQ_COUNT = 0, 1
+
+
+class Request(C.Structure):
+    _fields_ = [("type", C.c_int), ("eps", C.c_double), ("mu", C.c_int), ("graph", GenParams)]
+
+
+class Result(C.Structure):
+    _fields_ = [("status", C.c_int), ("type", C.c_int), ("queue_ms", C.c_double), ("run_ms", C.c_double),
+                ("latency_ms", C.c_double), ("summary", ScanSummary), ("n", C.c_uint64), ("m", C.c_uint64),
+                ("count_sum", C.c_uint64), ("count_digest", C.c_uint64)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "summary"}
+        d["summary"] = self.summary.as_dict()
+        return d
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("workers", C.c_int), ("hbm_budget", C.c_uint64), ("count_policy", C.c_int),
+                ("count_sm_percent", C.c_int)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
+                ("query_p50_ms", C.c_double), ("query_p99_ms", C.c_double), ("count_p50_ms", C.c_double),
+                ("count_p99_ms", C.c_double), ("elapsed_s", C.c_double), ("throughput_rps", C.c_double),
+                ("max_concurrent", C.c_int), ("peak_bytes", C.c_uint64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 def _load():
@@ -98,6 +132,17 @@ def _load():
         "accx_model_table_for": (C.c_int, [P, P, P]),
         "accx_graph_set_model": (C.c_int, [P, P]),
         "accx_batch_create": (C.c_int, [P, C.c_int, P, C.POINTER(P)]),
+        "accx_cn_digest": (C.c_int, [P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), P]),
+        "accx_query_ctx_create": (C.c_int, [P, C.POINTER(P)]),
+        "accx_query_ctx_free": (C.c_int, [P]),
+        "accx_server_create": (C.c_int, [P, C.POINTER(ServerConfig), C.POINTER(P)]),
+        "accx_server_submit": (C.c_int, [P, C.POINTER(Request), C.POINTER(C.c_uint64)]),
+        "accx_server_poll": (C.c_int, [P, C.c_uint64, C.POINTER(Result)]),
+        "accx_server_wait": (C.c_int, [P, C.c_uint64, C.c_double, C.POINTER(Result)]),
+        "accx_server_drain": (C.c_int, [P]),
+        "accx_server_stats_get": (C.c_int, [P, C.POINTER(ServerStats)]),
+        "accx_server_request_bytes": (C.c_uint64, [P, C.POINTER(Request)]),
+        "accx_server_destroy": (C.c_int, [P]),
         "accx_batch_free": (C.c_int, [P]),
         "accx_batch_union": (P, [P]),
         "accx_batch_graph_range": (C.c_int, [P, C.c_int, P, P, P, P]),
@@ -286,7 +331,8 @@ class Graph:
             tab = keep.ctypes.data_as(C.POINTER(C.c_uint8))
             if pol == POLICY_HEURISTIC and isinstance(policy, str) and policy == "heuristic":
                 pass
-        return CountOpts(pol, tab, int(bias), int(block_warps), int(window_kb), 1 if timing else 0, int(sparse_kb)), keep
+        return CountOpts(pol, tab, int(bias), int(block_warps), int(window_kb), 1 if timing else 0, int(sparse_kb),
+                         0), keep
 
     def count(self, policy="heuristic", table=None, bias=0, out="host", block_warps=0, window_kb=0, stream=None,
               timing=False, sparse_kb=0):
@@ -301,6 +347,12 @@ class Graph:
         _check(lib.accx_cn_count(self._h, C.byref(opts), target, _stream_ptr(stream)), "cn_count")
         del keep
         return None
+
+    def digest(self, stream=None):
+        """(sum, order-independent hash) of the resident counts."""
+        a, b = C.c_uint64(), C.c_uint64()
+        _check(lib.accx_cn_digest(self._h, C.byref(a), C.byref(b), _stream_ptr(stream)), "cn_digest")
+        return int(a.value), int(b.value)
 
     def read_counts(self, stream=None):
         """The resident counts (after a count or a captured replay), to the host."""
@@ -480,3 +532,63 @@ class Batch:
         for vb, n, eb, m in self.ranges:
             out.append(arr[eb:eb + m] if per == "entry" else arr[vb:vb + n])
         return out
+
+
+def query_request(eps, mu):
+    return Request(REQ_QUERY, float(eps), int(mu), GenParams())
+
+
+def count_request(params):
+    return Request(REQ_COUNT, 0.0, 0, params)
+
+
+class Server:
+    """accx_server: continuous batching of SCAN queries on a resident counted
+    graph and of new-graph count requests, admitted by an HBM budget."""
+
+    def __init__(self, resident, workers=4, hbm_budget=0, count_policy="bitmap", count_sm_percent=0):
+        self.resident = resident
+        pol = POLICIES[count_policy] if isinstance(count_policy, str) else int(count_policy)
+        cfg = ServerConfig(int(workers), int(hbm_budget), pol, int(count_sm_percent))
+        self._h = C.c_void_p()
+        _check(lib.accx_server_create(resident._h, C.byref(cfg), C.byref(self._h)), "server_create")
+
+    def submit(self, req):
+        i = C.c_uint64()
+        _check(lib.accx_server_submit(self._h, C.byref(req), C.byref(i)), "server_submit")
+        return int(i.value)
+
+    def poll(self, rid):
+        r = Result()
+        st = lib.accx_server_poll(self._h, int(rid), C.byref(r))
+        if st == ERR_NOT_READY:
+            return None
+        _check(st, "server_poll")
+        return r
+
+    def wait(self, rid, timeout_ms=-1.0):
+        r = Result()
+        _check(lib.accx_server_wait(self._h, int(rid), float(timeout_ms), C.byref(r)), "server_wait")
+        return r
+
+    def drain(self):
+        _check(lib.accx_server_drain(self._h), "server_drain")
+
+    def stats(self):
+        st = ServerStats()
+        _check(lib.accx_server_stats_get(self._h, C.byref(st)), "server_stats")
+        return st.as_dict()
+
+    def request_bytes(self, req):
+        return int(lib.accx_server_request_bytes(self._h, C.byref(req)))
+
+    def close(self):
+        if self._h:
+            lib.accx_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -12,13 +12,48 @@
 // a list's last window never leave the allocation.
 #define ACCX_DST_PAD 64
 
+// Scratch and results of one SCAN query; a graph handle owns one, and
+// accx_query_ctx_create makes more so that several queries can run on the same
+// resident graph at once (each on its own stream).
+struct accx_query_ctx {
+  uint32_t *d_simbits = nullptr;  // ceil(m/32) words
+  int32_t *d_core_count = nullptr;
+  int32_t *d_label = nullptr;
+  int32_t *d_parent = nullptr;
+  int32_t *d_hubmin = nullptr;
+  int32_t *d_hubmax = nullptr;
+  unsigned long long *d_qcounters = nullptr;  // query counters
+  uint32_t *d_corebits = nullptr;             // n bits: core flags of the last query
+  uint32_t *d_big = nullptr;                  // vertices whose rows are counted by a whole CTA
+  bool query_valid = false;
+  double last_eps = 0;
+  int last_mu = 0;
+  // pairs of the last query (built on demand)
+  unsigned long long *d_pairs = nullptr;
+  unsigned long long *d_pairs_tmp = nullptr;
+  uint64_t pairs_cap = 0;
+  uint64_t npairs = 0;
+  bool pairs_valid = false;
+  accx_scan_summary summary{};
+  uint32_t n = 0;   // sizes the arrays were made for
+  uint64_t m = 0;
+};
+void accx_query_ctx_release(accx_query_ctx *q);
+
 struct accx_graph {
   int device = 0;
+  // stream the handle was made on: when set, its device arrays come from and
+  // return to the stream-ordered allocator on it (no device-wide sync on free)
+  cudaStream_t home = nullptr;
   uint32_t n = 0;
   uint64_t m = 0;
   uint32_t *d_off = nullptr;  // n+1
   int32_t *d_dst = nullptr;   // m + ACCX_DST_PAD
   int32_t *d_cnt = nullptr;   // m
+  float *d_simkey = nullptr;    // m: similarity key per entry (built by the first query after a count)
+  bool key_valid = false;
+  uint32_t *d_tilerow = nullptr;   // row of every 256-entry tile's first entry (+1 for the last entry)
+  uint32_t *d_rtilerow = nullptr;  // the same for the relabeled CSR
   // degree-descending relabel (accx_graph_relabel): counting runs on these
   uint32_t *d_roff = nullptr;   // n+1
   int32_t *d_rdst = nullptr;    // m + ACCX_DST_PAD
@@ -42,24 +77,8 @@ struct accx_graph {
   cudaEvent_t ev[ACCX_NUM_PHASES + 1] = {};
   bool timed = false;
 
-  // SCAN query state
-  uint32_t *d_simbits = nullptr;  // ceil(m/32) words
-  int32_t *d_core_count = nullptr;
-  int32_t *d_label = nullptr;
-  int32_t *d_parent = nullptr;
-  int32_t *d_hubmin = nullptr;
-  int32_t *d_hubmax = nullptr;
-  unsigned long long *d_qcounters = nullptr;  // query counters
-  bool query_valid = false;
-  double last_eps = 0;
-  int last_mu = 0;
-  // pairs of the last query (built on demand)
-  unsigned long long *d_pairs = nullptr;
-  unsigned long long *d_pairs_tmp = nullptr;
-  uint64_t pairs_cap = 0;
-  uint64_t npairs = 0;
-  bool pairs_valid = false;
-  accx_scan_summary summary{};
+  // SCAN query state of the handle's own queries (accx_scan_query)
+  accx_query_ctx qc;
 
   // trained cost model state (accx_model_*)
   void *model = nullptr;
@@ -76,6 +95,11 @@ struct accx_graph {
   } while (0)
 
 void accx_set_cuda_error(cudaError_t e, const char *what, const char *file, int line);
+
+// Device memory on a stream's pool when s != NULL (no device-wide synchronisation
+// on free), else plain cudaMalloc/cudaFree.
+cudaError_t accx_dev_alloc(void **p, size_t bytes, cudaStream_t s);
+void accx_dev_free(void *p, cudaStream_t s);
 
 // True when p is a device (or managed) pointer.
 bool accx_is_device_ptr(const void *p);
@@ -98,6 +122,9 @@ int accx_model_table(accx_graph *g, uint8_t *table);
 int accx_model_table_device(accx_graph *g, cudaStream_t s);
 
 // Exclusive/inclusive helpers implemented in gen.cu.
+// Row index of every 256-entry tile of a CSR (graph.cu), allocated on g's home stream.
+int accx_tilerow_build(accx_graph *g, const uint32_t *off, uint32_t **out, cudaStream_t s);
+
 // Relabeled counts -> the handle's entry order (relabel.cu).
 int accx_relabel_gather(accx_graph *g, cudaStream_t s);
 

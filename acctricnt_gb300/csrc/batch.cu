@@ -95,7 +95,9 @@ extern "C" int accx_batch_create(accx_graph *const *graphs, int k, void *stream,
         cudaMemsetAsync(u->d_dst + M, 0xff, sizeof(int32_t) * ACCX_DST_PAD, s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
     dim3 grid(64, k < 65535 ? k : 65535);
     k_union<<<grid, 256, 0, s>>>(d_ds, k, u->d_off, u->d_dst);
-    if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
+    if (cudaGetLastError() != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
+    if ((rc = accx_tilerow_build(u, u->d_off, &u->d_tilerow, s)) != ACCX_OK) break;
+    if (cudaStreamSynchronize(s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
   } while (0);
   if (d_ds) cudaFree(d_ds);
   if (rc) {

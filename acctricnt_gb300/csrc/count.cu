@@ -56,7 +56,7 @@ __device__ __forceinline__ int accx_edge_kind(int policy, const uint8_t *table, 
 // ---------------------------------------------------------------------------
 // classify: one thread per CSR entry.
 template <int TILE>
-__global__ void __launch_bounds__(TILE) k_classify(const uint32_t *__restrict__ off, const int32_t *__restrict__ dst,
+__global__ void __launch_bounds__(TILE) k_classify(const uint32_t *__restrict__ off, const uint32_t *__restrict__ tilerow, const int32_t *__restrict__ dst,
                                                    uint32_t n, uint32_t m, int policy,
                                                    const uint8_t *__restrict__ table, uint2 *__restrict__ list,
                                                    uint32_t list_cap, unsigned long long *__restrict__ work_u,
@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(TILE) k_classify(const uint32_t *__restrict__ 
     for (int i = threadIdx.x; i < ACCX_NB * ACCX_NB; i += TILE) s_table[i] = table[i];
   uint32_t base = blockIdx.x * (uint32_t)TILE;
   uint32_t e = base + threadIdx.x;
-  uint32_t u = accx_tile_row<TILE>(off, n, m, base, e, &sh);  // contains __syncthreads
+  uint32_t u = accx_tile_row<TILE>(off, tilerow, n, m, base, e, &sh);  // contains __syncthreads
   int kind = -1;
   uint32_t v = 0, du = 0, dv = 0;
   if (e < m) {
@@ -517,12 +517,12 @@ __global__ void __launch_bounds__(1024, 1) k_bitmap(const uint32_t *__restrict__
 // Mirror: each owned entry e=(u,v) adds the bias and copies its count to the
 // reverse entry (the position of u in N(v)).
 template <int TILE>
-__global__ void __launch_bounds__(TILE) k_mirror(const uint32_t *__restrict__ off, const int32_t *__restrict__ dst,
+__global__ void __launch_bounds__(TILE) k_mirror(const uint32_t *__restrict__ off, const uint32_t *__restrict__ tilerow, const int32_t *__restrict__ dst,
                                                  uint32_t n, uint32_t m, int32_t bias, int32_t *__restrict__ cnt) {
   __shared__ accx_tile_rows<TILE> sh;
   uint32_t base = blockIdx.x * (uint32_t)TILE;
   uint32_t e = base + threadIdx.x;
-  uint32_t u = accx_tile_row<TILE>(off, n, m, base, e, &sh);
+  uint32_t u = accx_tile_row<TILE>(off, tilerow, n, m, base, e, &sh);
   if (e >= m) return;
   uint32_t v = (uint32_t)dst[e];
   uint32_t du = off[u + 1] - off[u];
@@ -537,22 +537,26 @@ __global__ void __launch_bounds__(TILE) k_mirror(const uint32_t *__restrict__ of
 // ---------------------------------------------------------------------------
 int accx_ensure_count_scratch(accx_graph *g) {
   const size_t m = g->m, n = g->n;
-  if (!g->d_cnt) ACCX_CUDA_TRY(cudaMalloc(&g->d_cnt, sizeof(int32_t) * (m ? m : 1)));
-  if (!g->d_edge_list) ACCX_CUDA_TRY(cudaMalloc(&g->d_edge_list, sizeof(uint2) * (m / 2 + 1)));
+  cudaStream_t h = g->home;
+  if (!g->d_cnt) ACCX_CUDA_TRY(accx_dev_alloc((void **)&g->d_cnt, sizeof(int32_t) * (m ? m : 1), h));
+  if (!g->d_edge_list) ACCX_CUDA_TRY(accx_dev_alloc((void **)&g->d_edge_list, sizeof(uint2) * (m / 2 + 1), h));
   if (!g->d_icnt) {
-    ACCX_CUDA_TRY(cudaMalloc(&g->d_icnt, sizeof(unsigned long long) * (n + 1)));
-    ACCX_CUDA_TRY(cudaMalloc(&g->d_prefix, sizeof(unsigned long long) * (n + 1)));
+    ACCX_CUDA_TRY(accx_dev_alloc((void **)&g->d_icnt, sizeof(unsigned long long) * (n + 1), h));
+    ACCX_CUDA_TRY(accx_dev_alloc((void **)&g->d_prefix, sizeof(unsigned long long) * (n + 1), h));
     size_t bytes = 0;
     ACCX_CUDA_TRY(cub::DeviceScan::ExclusiveSum(nullptr, bytes, g->d_icnt, g->d_prefix, (int64_t)n + 1));
-    ACCX_CUDA_TRY(cudaMalloc(&g->d_scan_tmp, bytes ? bytes : 16));
+    ACCX_CUDA_TRY(accx_dev_alloc(&g->d_scan_tmp, bytes ? bytes : 16, h));
     g->scan_tmp_bytes = bytes;
   }
   if (!g->d_counters) {
     // counters followed by the per-vertex bitmap work array
-    ACCX_CUDA_TRY(cudaMalloc(&g->d_counters, sizeof(unsigned long long) * (C_NUM + n + 1)));
-    ACCX_CUDA_TRY(cudaMemset(g->d_counters, 0, sizeof(unsigned long long) * (C_NUM + n + 1)));
+    ACCX_CUDA_TRY(accx_dev_alloc((void **)&g->d_counters, sizeof(unsigned long long) * (C_NUM + n + 1), h));
   }
-  if (!g->d_table) ACCX_CUDA_TRY(cudaMalloc(&g->d_table, ACCX_NB * ACCX_NB));
+  if (!g->d_table) {
+    ACCX_CUDA_TRY(accx_dev_alloc((void **)&g->d_table, ACCX_NB * ACCX_NB, h));
+    // pool allocations are ordered on the home stream; counts may run on another
+    if (h) ACCX_CUDA_TRY(cudaStreamSynchronize(h));
+  }
   return ACCX_OK;
 }
 
@@ -593,6 +597,7 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s)
   const uint32_t *off = rel ? g->d_roff : g->d_off;
   const int32_t *dst = rel ? g->d_rdst : g->d_dst;
   int32_t *cnt = rel ? g->d_rcnt : g->d_cnt;
+  const uint32_t *tilerow = rel ? g->d_rtilerow : g->d_tilerow;
   unsigned long long *ctr = g->d_counters;
   unsigned long long *work_u = g->d_counters + C_NUM;
   ACCX_CUDA_TRY(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long) * (C_NUM + (size_t)n + 1), s));
@@ -611,8 +616,9 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s)
 #define ACCX_MARK(i) \
   if (timing) ACCX_CUDA_TRY(cudaEventRecord(g->ev[i], s));
   ACCX_MARK(0);
-  k_classify<256><<<tiles, 256, 0, s>>>(off, dst, n, m, policy, g->d_table, g->d_edge_list, list_cap, work_u, ctr);
-  const int sms = accx_sm_count(g->device);
+  k_classify<256><<<tiles, 256, 0, s>>>(off, tilerow, dst, n, m, policy, g->d_table, g->d_edge_list, list_cap, work_u, ctr);
+  int sms = accx_sm_count(g->device);
+  if (o && o->sm_limit > 0 && o->sm_limit < sms) sms = o->sm_limit;
   const uint32_t W = (uint32_t)dkb * 8192u;        // dense ids (bits)
   const uint32_t S = (uint32_t)skb * 1024u / 8u;   // sparse 8-byte slots
   const size_t smem = (size_t)W / 8u + (size_t)S * 8u;
@@ -632,7 +638,7 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s)
   k_bitmap<<<sms * per_sm, warps * 32, smem, s>>>(off, dst, n, policy, g->d_table, work_u, g->d_prefix, W, S, target,
                                                   cnt);
   ACCX_MARK(4);
-  k_mirror<256><<<tiles, 256, 0, s>>>(off, dst, n, m, bias, cnt);
+  k_mirror<256><<<tiles, 256, 0, s>>>(off, tilerow, dst, n, m, bias, cnt);
   if (rel) {
     rc = accx_relabel_gather(g, s);
     if (rc) return rc;
@@ -642,8 +648,9 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s)
   ACCX_CUDA_TRY(cudaGetLastError());
   g->cnt_bias = bias;
   g->cnt_valid = true;
-  g->query_valid = false;
-  g->pairs_valid = false;
+  g->qc.query_valid = false;
+  g->qc.pairs_valid = false;
+  g->key_valid = false;
   return ACCX_OK;
 }
 

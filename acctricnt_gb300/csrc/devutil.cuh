@@ -25,22 +25,32 @@ __device__ __forceinline__ uint32_t accx_lower_bound(const int32_t *__restrict__
   return b;
 }
 
-// Entry tiles: a CTA of TILE threads maps entries [base, base+TILE) to rows with
-// one search over the whole offset array (two threads) and one short search per
-// thread inside the rows the tile spans.
+// Entry tiles: a CTA of TILE threads maps entries [base, base+TILE) to rows.
+// With `tilerow` (row of every tile's first entry, built once per CSR by
+// accx_tilerow_build) the CTA reads its row range; without it two threads
+// search the whole offset array.  Each thread then searches only the rows the
+// tile spans.  Launch one CTA per tile (blockIdx.x = tile).
 template <int TILE>
 struct accx_tile_rows {
   uint32_t r_lo, r_hi;
 };
 
 template <int TILE>
-__device__ __forceinline__ uint32_t accx_tile_row(const uint32_t *__restrict__ off, uint32_t n, uint32_t m,
+__device__ __forceinline__ uint32_t accx_tile_row(const uint32_t *__restrict__ off,
+                                                  const uint32_t *__restrict__ tilerow, uint32_t n, uint32_t m,
                                                   uint32_t base, uint32_t e, accx_tile_rows<TILE> *sh) {
-  if (threadIdx.x == 0) sh->r_lo = accx_row_of(off, 0, n, base);
-  if (threadIdx.x == 1 || blockDim.x == 1) {
-    uint32_t last = base + TILE - 1;
-    if (last >= m) last = m - 1;
-    sh->r_hi = accx_row_of(off, 0, n, last);
+  if (tilerow) {
+    if (threadIdx.x == 0) {
+      sh->r_lo = __ldg(tilerow + blockIdx.x);
+      sh->r_hi = __ldg(tilerow + blockIdx.x + 1);
+    }
+  } else {
+    if (threadIdx.x == 0) sh->r_lo = accx_row_of(off, 0, n, base);
+    if (threadIdx.x == 1 || blockDim.x == 1) {
+      uint32_t last = base + TILE - 1;
+      if (last >= m) last = m - 1;
+      sh->r_hi = accx_row_of(off, 0, n, last);
+    }
   }
   __syncthreads();
   uint32_t r = 0;

@@ -54,13 +54,13 @@ int accx_build_csr_from_keys(accx_graph *g, unsigned long long *d_keys, uint64_t
   unsigned long long *d_nsel = nullptr;
   int rc = ACCX_OK;
   do {
-    if (cudaMalloc(&d_alt, sizeof(unsigned long long) * (nkeys ? nkeys : 1)) != cudaSuccess) { rc = ACCX_ERR_OOM; break; }
+    if (accx_dev_alloc((void **)&d_alt, sizeof(unsigned long long) * (nkeys ? nkeys : 1), s) != cudaSuccess) { rc = ACCX_ERR_OOM; break; }
     cub::DoubleBuffer<unsigned long long> db(d_keys, d_alt);
     if (cub::DeviceRadixSort::SortKeys(nullptr, tmp_bytes, db, (int64_t)nkeys, 0, 64, s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
     if (cub::DeviceSelect::Unique(nullptr, tmp2, d_keys, d_alt, d_nsel, (int64_t)nkeys, s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
     if (tmp2 > tmp_bytes) tmp_bytes = tmp2;
-    if (cudaMalloc(&d_tmp, tmp_bytes ? tmp_bytes : 1) != cudaSuccess) { rc = ACCX_ERR_OOM; break; }
-    if (cudaMalloc(&d_nsel, sizeof(unsigned long long)) != cudaSuccess) { rc = ACCX_ERR_OOM; break; }
+    if (accx_dev_alloc(&d_tmp, tmp_bytes ? tmp_bytes : 1, s) != cudaSuccess) { rc = ACCX_ERR_OOM; break; }
+    if (accx_dev_alloc((void **)&d_nsel, sizeof(unsigned long long), s) != cudaSuccess) { rc = ACCX_ERR_OOM; break; }
     if (cub::DeviceRadixSort::SortKeys(d_tmp, tmp_bytes, db, (int64_t)nkeys, 0, 64, s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
     unsigned long long *sorted = db.Current();
     d_uniq = db.Alternate();
@@ -76,17 +76,19 @@ int accx_build_csr_from_keys(accx_graph *g, unsigned long long *d_keys, uint64_t
     if (nu >= (1ull << 32) - ACCX_DST_PAD) { rc = ACCX_ERR_TOO_LARGE; break; }
     g->n = n;
     g->m = nu;
-    if (cudaMalloc(&g->d_off, sizeof(uint32_t) * ((size_t)n + 1)) != cudaSuccess ||
-        cudaMalloc(&g->d_dst, sizeof(int32_t) * ((size_t)nu + ACCX_DST_PAD)) != cudaSuccess) { rc = ACCX_ERR_OOM; break; }
+    if (accx_dev_alloc((void **)&g->d_off, sizeof(uint32_t) * ((size_t)n + 1), g->home) != cudaSuccess ||
+        accx_dev_alloc((void **)&g->d_dst, sizeof(int32_t) * ((size_t)nu + ACCX_DST_PAD), g->home) != cudaSuccess) { rc = ACCX_ERR_OOM; break; }
     if (cudaMemsetAsync(g->d_dst + nu, 0xff, sizeof(int32_t) * ACCX_DST_PAD, s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
     int grid = accx_grid_for(g->device, 256, 8);
     k_keys_to_csr<<<grid, 256, 0, s>>>(d_uniq, nu, n, g->d_off, g->d_dst);
-    if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
+    if (cudaGetLastError() != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
+    if ((rc = accx_tilerow_build(g, g->d_off, &g->d_tilerow, s)) != ACCX_OK) break;
+    if (cudaStreamSynchronize(s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
   } while (0);
   if (rc == ACCX_ERR_CUDA || rc == ACCX_ERR_OOM) cudaGetLastError();
-  if (d_alt) cudaFree(d_alt);
-  if (d_tmp) cudaFree(d_tmp);
-  if (d_nsel) cudaFree(d_nsel);
+  accx_dev_free(d_alt, s);
+  accx_dev_free(d_tmp, s);
+  accx_dev_free(d_nsel, s);
   return rc;
 }
 
@@ -106,16 +108,17 @@ extern "C" int accx_graph_generate(const accx_gen_params *p, void *stream, accx_
   accx_graph *g = new (std::nothrow) accx_graph();
   if (!g) return ACCX_ERR_OOM;
   cudaGetDevice(&g->device);
+  g->home = s;
   unsigned long long *d_keys = nullptr;
   uint64_t *d_cdf = nullptr;
   do {
-    if (cudaMalloc(&d_keys, sizeof(unsigned long long) * draws * 2) != cudaSuccess) { rc = ACCX_ERR_OOM; break; }
+    if (accx_dev_alloc((void **)&d_keys, sizeof(unsigned long long) * draws * 2, s) != cudaSuccess) { rc = ACCX_ERR_OOM; break; }
     accx_rmat_thresholds t{};
     if (p->kind == ACCX_GEN_RMAT) t = accx_rmat_make(p->q0, p->q1, p->q2);
     if (p->kind == ACCX_GEN_CHUNG_LU) {
       std::vector<uint64_t> cdf;
       accx_chung_lu_cdf(n, draws, p->q0, p->q1, cdf);
-      if (cudaMalloc(&d_cdf, sizeof(uint64_t) * cdf.size()) != cudaSuccess) { rc = ACCX_ERR_OOM; break; }
+      if (accx_dev_alloc((void **)&d_cdf, sizeof(uint64_t) * cdf.size(), s) != cudaSuccess) { rc = ACCX_ERR_OOM; break; }
       if (cudaMemcpyAsync(d_cdf, cdf.data(), sizeof(uint64_t) * cdf.size(), cudaMemcpyHostToDevice, s) != cudaSuccess ||
           cudaStreamSynchronize(s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
     }
@@ -126,8 +129,8 @@ extern "C" int accx_graph_generate(const accx_gen_params *p, void *stream, accx_
     rc = accx_build_csr_from_keys(g, d_keys, draws * 2, n, s);
   } while (0);
   if (rc == ACCX_ERR_CUDA || rc == ACCX_ERR_OOM) cudaGetLastError();
-  if (d_keys) cudaFree(d_keys);
-  if (d_cdf) cudaFree(d_cdf);
+  accx_dev_free(d_keys, s);
+  accx_dev_free(d_cdf, s);
   if (rc) {
     accx_graph_free(g);
     return rc;

@@ -46,6 +46,16 @@ extern "C" const char *accx_strerror(int status) {
 
 extern "C" const char *accx_version(void) { return ACCX_VERSION_STR; }
 
+cudaError_t accx_dev_alloc(void **p, size_t bytes, cudaStream_t s) {
+  return s ? cudaMallocAsync(p, bytes, s) : cudaMalloc(p, bytes);
+}
+
+void accx_dev_free(void *p, cudaStream_t s) {
+  if (!p) return;
+  if (s) cudaFreeAsync(p, s);
+  else cudaFree(p);
+}
+
 bool accx_is_device_ptr(const void *p) {
   if (!p) return false;
   cudaPointerAttributes a;
@@ -95,12 +105,12 @@ int accx_grid_for(int device, int block, int per_sm) {
 #define V_ASYM 8
 // Range checks always run (every kernel indexes off[] with neighbour ids); the
 // order, self-loop and symmetry checks run when `full` is set.
-__global__ void k_validate(const uint32_t *__restrict__ off, const int32_t *__restrict__ dst, uint32_t n,
+__global__ void k_validate(const uint32_t *__restrict__ off, const uint32_t *__restrict__ tilerow, const int32_t *__restrict__ dst, uint32_t n,
                            uint32_t m, int full, int *__restrict__ status) {
   __shared__ accx_tile_rows<256> sh;
   uint32_t base = blockIdx.x * 256u;
   uint32_t e = base + threadIdx.x;
-  uint32_t u = accx_tile_row<256>(off, n, m, base, e, &sh);
+  uint32_t u = accx_tile_row<256>(off, tilerow, n, m, base, e, &sh);
   if (e >= m) return;
   int32_t v = dst[e];
   if (v < 0 || (uint32_t)v >= n) { atomicOr(status, V_RANGE); return; }
@@ -110,6 +120,28 @@ __global__ void k_validate(const uint32_t *__restrict__ off, const int32_t *__re
   uint32_t b = off[v], t = off[v + 1];
   uint32_t r = accx_lower_bound(dst, b, t, (int32_t)u);
   if (r >= t || dst[r] != (int32_t)u) atomicOr(status, V_ASYM);
+}
+
+__global__ void k_tilerow(const uint32_t *__restrict__ off, uint32_t n, uint32_t m, uint32_t ntiles,
+                          uint32_t *__restrict__ tr) {
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t <= ntiles; t += gridDim.x * blockDim.x) {
+    uint32_t e = t < ntiles ? t * 256u : m - 1;
+    if (e >= m) e = m - 1;
+    tr[t] = accx_row_of(off, 0, n, e);
+  }
+}
+
+int accx_tilerow_build(accx_graph *g, const uint32_t *off, uint32_t **out, cudaStream_t s) {
+  const uint32_t m = (uint32_t)g->m;
+  if (m == 0 || *out) return ACCX_OK;
+  const uint32_t ntiles = (m + 255) / 256;
+  uint32_t *p = nullptr;
+  ACCX_CUDA_TRY(accx_dev_alloc((void **)&p, sizeof(uint32_t) * ((size_t)ntiles + 2), g->home));
+  if (g->home && g->home != s) ACCX_CUDA_TRY(cudaStreamSynchronize(g->home));
+  k_tilerow<<<accx_sm_count(g->device) * 8, 256, 0, s>>>(off, g->n, m, ntiles, p);
+  ACCX_CUDA_TRY(cudaGetLastError());
+  *out = p;
+  return ACCX_OK;
 }
 
 static int check_offsets_host(const uint32_t *off, uint32_t n, uint64_t m) {
@@ -138,9 +170,10 @@ int accx_graph_validate_device(accx_graph *g, int full, cudaStream_t s) {
     if (cudaMemcpyAsync(&st, d_status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
     if (st) { rc = ACCX_ERR_RANGE; break; }
+    if ((rc = accx_tilerow_build(g, g->d_off, &g->d_tilerow, s)) != ACCX_OK) break;
     if (g->m) {
       uint32_t blocks = (uint32_t)((g->m + 255) / 256);
-      k_validate<<<blocks, 256, 0, s>>>(g->d_off, g->d_dst, g->n, (uint32_t)g->m, full, d_status);
+      k_validate<<<blocks, 256, 0, s>>>(g->d_off, g->d_tilerow, g->d_dst, g->n, (uint32_t)g->m, full, d_status);
       if (cudaMemcpyAsync(&st, d_status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
           cudaStreamSynchronize(s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
       rc = (st & V_RANGE) ? ACCX_ERR_RANGE : (st & V_SELF) ? ACCX_ERR_SELF_LOOP
@@ -250,12 +283,11 @@ extern "C" int accx_graph_load_dir(const char *dir, unsigned flags, void *stream
 
 extern "C" int accx_graph_free(accx_graph *g) {
   if (!g) return ACCX_ERR_INVALID_ARG;
-  void *ptrs[] = {g->d_off,       g->d_dst,   g->d_cnt,       g->d_edge_list, g->d_icnt, g->d_prefix, g->d_scan_tmp,
-                  g->d_counters,  g->d_table, g->d_simbits,   g->d_core_count, g->d_label,
-                  g->d_parent,    g->d_hubmin, g->d_hubmax,   g->d_qcounters,  g->d_pairs,
-                  g->d_pairs_tmp, g->d_roff, g->d_rdst, g->d_rmap, g->d_rcnt, g->d_oldid, g->d_newid};
-  for (void *p : ptrs)
-    if (p) cudaFree(p);
+  void *ptrs[] = {g->d_off,      g->d_dst,    g->d_cnt,  g->d_edge_list, g->d_icnt,  g->d_prefix, g->d_scan_tmp,
+                  g->d_counters, g->d_table,  g->d_roff, g->d_rdst,      g->d_rmap,  g->d_rcnt,   g->d_oldid,
+                  g->d_newid,    g->d_simkey, g->d_tilerow, g->d_rtilerow};
+  accx_query_ctx_release(&g->qc);
+  for (void *p : ptrs) accx_dev_free(p, g->home);
   for (int i = 0; i <= ACCX_NUM_PHASES; i++)
     if (g->ev[i]) cudaEventDestroy(g->ev[i]);
   accx_model_release(g);

@@ -195,14 +195,14 @@ __global__ void __launch_bounds__(256) k_model_infer(const __half *__restrict__ 
 // Bucket statistics over owned edges: per block shared histograms, then global.
 #define NBB (ACCX_NB * ACCX_NB)
 template <int TILE>
-__global__ void __launch_bounds__(TILE) k_bucket_stats(const uint32_t *__restrict__ off, const int32_t *__restrict__ dst,
+__global__ void __launch_bounds__(TILE) k_bucket_stats(const uint32_t *__restrict__ off, const uint32_t *__restrict__ tilerow, const int32_t *__restrict__ dst,
                                                        uint32_t n, uint32_t m, unsigned long long *__restrict__ st) {
   __shared__ accx_tile_rows<TILE> sh;
   __shared__ unsigned long long hs[3 * NBB];
   for (int i = threadIdx.x; i < 3 * NBB; i += TILE) hs[i] = 0;
   uint32_t base = blockIdx.x * (uint32_t)TILE;
   uint32_t e = base + threadIdx.x;
-  uint32_t u = accx_tile_row<TILE>(off, n, m, base, e, &sh);  // contains __syncthreads
+  uint32_t u = accx_tile_row<TILE>(off, tilerow, n, m, base, e, &sh);  // contains __syncthreads
   if (e < m) {
     uint32_t v = (uint32_t)dst[e];
     uint32_t du = off[u + 1] - off[u], dv = off[v + 1] - off[v];
@@ -272,7 +272,7 @@ static int ensure_features(accx_graph *g, cudaStream_t s) {
   if (!st->d_feat) ACCX_CUDA_TRY(cudaMalloc(&st->d_feat, sizeof(float) * NBB * IN));
   ACCX_CUDA_TRY(cudaMemsetAsync(st->d_stats, 0, sizeof(unsigned long long) * 3 * NBB, s));
   const uint32_t m = (uint32_t)g->m;
-  if (m) k_bucket_stats<256><<<(m + 255) / 256, 256, 0, s>>>(g->d_off, g->d_dst, g->n, m, st->d_stats);
+  if (m) k_bucket_stats<256><<<(m + 255) / 256, 256, 0, s>>>(g->d_off, g->d_tilerow, g->d_dst, g->n, m, st->d_stats);
   k_features<<<(NBB + 127) / 128, 128, 0, s>>>(st->d_stats, g->n, g->m, st->d_feat);
   ACCX_CUDA_TRY(cudaGetLastError());
   st->ready = true;

@@ -35,7 +35,7 @@ __global__ void __launch_bounds__(TILE) k_noalloc_classify(const uint32_t *__res
   __shared__ accx_tile_rows<TILE> sh;
   uint32_t base = blockIdx.x * (uint32_t)TILE;
   uint32_t e = base + threadIdx.x;
-  uint32_t u = accx_tile_row<TILE>(off, n, m, base, e, &sh);
+  uint32_t u = accx_tile_row<TILE>(off, nullptr, n, m, base, e, &sh);
   bool own = false;
   if (e < m) {
     uint32_t v = (uint32_t)dst[e];

@@ -31,14 +31,14 @@ __global__ void k_perm(const unsigned long long *__restrict__ sorted, uint32_t n
 }
 
 template <int TILE>
-__global__ void __launch_bounds__(TILE) k_entry_keys(const uint32_t *__restrict__ off, const int32_t *__restrict__ dst,
+__global__ void __launch_bounds__(TILE) k_entry_keys(const uint32_t *__restrict__ off, const uint32_t *__restrict__ tilerow, const int32_t *__restrict__ dst,
                                                      uint32_t n, uint32_t m, const uint32_t *__restrict__ newid,
                                                      unsigned long long *__restrict__ keys,
                                                      uint32_t *__restrict__ vals) {
   __shared__ accx_tile_rows<TILE> sh;
   uint32_t base = blockIdx.x * (uint32_t)TILE;
   uint32_t e = base + threadIdx.x;
-  uint32_t u = accx_tile_row<TILE>(off, n, m, base, e, &sh);
+  uint32_t u = accx_tile_row<TILE>(off, tilerow, n, m, base, e, &sh);
   if (e >= m) return;
   keys[e] = ((unsigned long long)newid[u] << 32) | newid[(uint32_t)dst[e]];
   vals[e] = e;
@@ -83,15 +83,16 @@ extern "C" int accx_graph_relabel(accx_graph *g, void *stream) {
         cudaMalloc(&k2, sizeof(unsigned long long) * big) != cudaSuccess ||
         cudaMalloc(&v1, sizeof(uint32_t) * big) != cudaSuccess || cudaMalloc(&v2, sizeof(uint32_t) * big) != cudaSuccess ||
         cudaMalloc(&rdeg, sizeof(uint32_t) * ((size_t)n + 1)) != cudaSuccess ||
-        cudaMalloc(&g->d_roff, sizeof(uint32_t) * ((size_t)n + 1)) != cudaSuccess ||
-        cudaMalloc(&g->d_rdst, sizeof(int32_t) * ((size_t)m + ACCX_DST_PAD)) != cudaSuccess ||
-        cudaMalloc(&g->d_rmap, sizeof(uint32_t) * ((size_t)m + 1)) != cudaSuccess ||
-        cudaMalloc(&g->d_rcnt, sizeof(int32_t) * ((size_t)m + 1)) != cudaSuccess ||
-        cudaMalloc(&g->d_oldid, sizeof(uint32_t) * ((size_t)n + 1)) != cudaSuccess ||
-        cudaMalloc(&g->d_newid, sizeof(uint32_t) * ((size_t)n + 1)) != cudaSuccess) {
+        accx_dev_alloc((void **)&g->d_roff, sizeof(uint32_t) * ((size_t)n + 1), g->home) != cudaSuccess ||
+        accx_dev_alloc((void **)&g->d_rdst, sizeof(int32_t) * ((size_t)m + ACCX_DST_PAD), g->home) != cudaSuccess ||
+        accx_dev_alloc((void **)&g->d_rmap, sizeof(uint32_t) * ((size_t)m + 1), g->home) != cudaSuccess ||
+        accx_dev_alloc((void **)&g->d_rcnt, sizeof(int32_t) * ((size_t)m + 1), g->home) != cudaSuccess ||
+        accx_dev_alloc((void **)&g->d_oldid, sizeof(uint32_t) * ((size_t)n + 1), g->home) != cudaSuccess ||
+        accx_dev_alloc((void **)&g->d_newid, sizeof(uint32_t) * ((size_t)n + 1), g->home) != cudaSuccess) {
       rc = ACCX_ERR_OOM;
       break;
     }
+    if (g->home && cudaStreamSynchronize(g->home) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
     size_t b1 = 0, b2 = 0, b3 = 0;
     cub::DoubleBuffer<unsigned long long> dk(k1, k2);
     cub::DoubleBuffer<uint32_t> dv(v1, v2);
@@ -115,11 +116,12 @@ extern "C" int accx_graph_relabel(accx_graph *g, void *stream) {
     // 2. entries: (new u, new v) keys carrying the original entry index
     dk = cub::DoubleBuffer<unsigned long long>(k1, k2);
     if (m) {
-      k_entry_keys<256><<<(m + 255) / 256, 256, 0, s>>>(g->d_off, g->d_dst, n, m, g->d_newid, k1, v1);
+      k_entry_keys<256><<<(m + 255) / 256, 256, 0, s>>>(g->d_off, g->d_tilerow, g->d_dst, n, m, g->d_newid, k1, v1);
       if (cub::DeviceRadixSort::SortPairs(tmp, tb, dk, dv, (int64_t)m, 0, 64, s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
       k_unpack_entries<<<grid, 256, 0, s>>>(dk.Current(), dv.Current(), m, g->d_rdst, g->d_rmap);
     }
     if (cudaMemsetAsync(g->d_rdst + m, 0xff, sizeof(int32_t) * ACCX_DST_PAD, s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
+    if ((rc = accx_tilerow_build(g, g->d_roff, &g->d_rtilerow, s)) != ACCX_OK) break;
     if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
   } while (0);
   if (rc) cudaGetLastError();
@@ -127,8 +129,8 @@ extern "C" int accx_graph_relabel(accx_graph *g, void *stream) {
     if (p) cudaFree(p);
   if (rc) {
     for (void **p : {(void **)&g->d_roff, (void **)&g->d_rdst, (void **)&g->d_rmap, (void **)&g->d_rcnt,
-                     (void **)&g->d_oldid, (void **)&g->d_newid}) {
-      if (*p) cudaFree(*p);
+                     (void **)&g->d_oldid, (void **)&g->d_newid, (void **)&g->d_rtilerow}) {
+      accx_dev_free(*p, g->home);
       *p = nullptr;
     }
   }

@@ -46,7 +46,14 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="rmat24", choices=["rmat24", "batch"])
+    ap.add_argument("--workload", default="rmat24", choices=["rmat24", "batch", "serve"])
+    ap.add_argument("--serve-scale", type=int, default=26)
+    ap.add_argument("--serve-rate", type=float, default=10.0)
+    ap.add_argument("--serve-requests", type=int, default=200)
+    ap.add_argument("--serve-workers", type=int, default=4)
+    ap.add_argument("--serve-budget-gb", type=float, default=64.0)
+    ap.add_argument("--serve-check", type=int, default=40)
+    ap.add_argument("--count-frac", type=float, default=0.1)
     ap.add_argument("--batch-k", type=int, default=512)
     ap.add_argument("--no-regret", dest="regret", action="store_false",
                     help="skip the exhaustive per-bucket timing that measures the scheduler's regret")
@@ -481,8 +488,89 @@ def run_batch(args):
         print(json.dumps(line), flush=True)
 
 
+def run_serve(args):
+    """Serving: a resident counted R-MAT graph; a Poisson stream of SCAN queries
+    (eps ~ U[0.1, 0.9], mu ~ U{2..20}) mixed with new-graph count requests
+    (R-MAT scale U{14..22}), admitted by an HBM budget."""
+    import torch
+    from acctricnt_gb300 import accx, sched
+    rank, world, local = dist_setup(args)
+    t0 = time.perf_counter()
+    G = accx.Graph.generate(accx.rmat_params(args.serve_scale, 16, seed=1 + rank))
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    G.relabel()
+    model, info = sched.default_model()
+    G.set_model(model)
+    G.count(policy="model", out=None)
+    torch.cuda.synchronize()
+    count_s = time.perf_counter() - t0
+    rng = np.random.default_rng(7 + rank)
+    reqs = []
+    for i in range(args.serve_requests):
+        if rng.random() < args.count_frac:
+            reqs.append(accx.count_request(accx.rmat_params(int(rng.integers(14, 23)), 16, seed=1000 + i)))
+        else:
+            reqs.append(accx.query_request(float(rng.uniform(0.1, 0.9)), int(rng.integers(2, 21))))
+    gaps = rng.exponential(1.0 / args.serve_rate, len(reqs))
+    S = accx.Server(G, workers=args.serve_workers, hbm_budget=int(args.serve_budget_gb * (1 << 30)),
+                    count_policy="bitmap")
+    for r in reqs[:4]:  # warm each path once (contexts, per-graph arrays)
+        S.wait(S.submit(r))
+    S.close()
+    S = accx.Server(G, workers=args.serve_workers, hbm_budget=int(args.serve_budget_gb * (1 << 30)),
+                    count_policy="bitmap")
+    ids = []
+    t_start = time.perf_counter()
+    t_next = t_start
+    for r, gap in zip(reqs, gaps):
+        t_next += gap
+        while time.perf_counter() < t_next:
+            time.sleep(min(0.0005, max(0.0, t_next - time.perf_counter())))
+        ids.append(S.submit(r))
+    S.drain()
+    res = [S.wait(i) for i in ids]
+    st = S.stats()
+    S.close()
+    # the same requests alone, one at a time: results must be identical
+    k = min(len(reqs), args.serve_check)
+    A = accx.Server(G, workers=1, hbm_budget=int(args.serve_budget_gb * (1 << 30)), count_policy="bitmap")
+    alone = [A.wait(A.submit(r)) for r in reqs[:k]]
+    A.close()
+
+    def key(r):
+        s = r.summary
+        return (r.status, s.cores, s.clusters, s.hubs, s.outliers, s.similar_entries, s.digest, r.n, r.m,
+                r.count_sum, r.count_digest)
+
+    same = all(key(a) == key(b) for a, b in zip(alone, res[:k]))
+    qlat = sorted(r.latency_ms for r in res if r.type == accx.REQ_QUERY)
+    qrun = sorted(r.run_ms for r in res if r.type == accx.REQ_QUERY)
+    pct = lambda v, p: round(v[min(len(v) - 1, int(round(p * (len(v) - 1))))], 3) if v else None
+    line = {"metric": "SCAN serving p50/p99 ms (continuous batching)", "value": round(st["query_p99_ms"], 3),
+            "unit": "ms", "n_gpus": world, "higher_is_better": False, "data": "synthetic",
+            "config": {"workload": "resident R-MAT scale %d ef 16 seed %d; Poisson %.1f req/s, %d requests, %.0f%% "
+                                   "new-graph counts (R-MAT scale 14-22), queries eps~U[0.1,0.9] mu~U{2..20}"
+                                   % (args.serve_scale, 1 + rank, args.serve_rate, len(reqs), 100 * args.count_frac),
+                       "n": G.n, "m": G.m, "workers": args.serve_workers, "hbm_budget_gb": args.serve_budget_gb,
+                       "resident_gen_s": round(gen_s, 2), "resident_count_s": round(count_s, 2)},
+            "query": {"p50_ms": st["query_p50_ms"], "p99_ms": st["query_p99_ms"], "run_p50_ms": pct(qrun, 0.5),
+                      "run_p99_ms": pct(qrun, 0.99), "n": len(qlat)},
+            "count": {"p50_ms": st["count_p50_ms"], "p99_ms": st["count_p99_ms"],
+                      "n": sum(1 for r in res if r.type == accx.REQ_COUNT)},
+            "throughput_rps": round(st["throughput_rps"], 2), "max_concurrent": st["max_concurrent"],
+            "peak_budget_gb": round(st["peak_bytes"] / (1 << 30), 2), "failed": st["failed"],
+            "same_alone_and_mixed": {"checked": k, "identical": bool(same)}}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "serve":
+        run_serve(args)
+        return
     if args.workload == "batch":
         run_batch(args)
     elif args.impl == "reference":

@@ -103,6 +103,9 @@ typedef struct {
   uint64_t seed;
 } accx_gen_params;
 
+/* A handle generated on a non-NULL stream takes its device arrays from that
+ * stream's memory pool and returns them there on accx_graph_free (no device-wide
+ * synchronisation); keep that stream alive until the handle is freed. */
 int accx_graph_generate(const accx_gen_params *params, void *stream, accx_graph **out);
 
 /* Host generator with the same output, for tests and for files.  Two calls:
@@ -141,6 +144,8 @@ typedef struct {
   int bitmap_window_kb;   /* dense shared-memory bitmap over the lowest ids, KiB (0 = tuned default) */
   int timing;             /* 1: record CUDA events around each phase (accx_cn_last_timings) */
   int sparse_table_kb;    /* hashed bitmap-word table for the other ids, KiB (0 = tuned default) */
+  int sm_limit;           /* run the persistent counting kernels on at most this many SMs (0 = all);
+                             leaves SMs free for latency-critical work on other streams */
 } accx_count_opts;
 
 /* Counts cnt[e] = |N(u) ∩ N(v)| + bias for every CSR entry e=(u,v) into the
@@ -151,6 +156,10 @@ int accx_cn_count(accx_graph *g, const accx_count_opts *opts, int32_t *out, void
 /* Copies the resident counts of the last count (or captured replay) to `out`
  * (host or device), without counting again. */
 int accx_cn_read(const accx_graph *g, int32_t *out, void *stream);
+
+/* Sum of the resident counts and an order-independent hash of every
+ * (entry, count) pair: a compact fingerprint for comparing two count runs. */
+int accx_cn_digest(const accx_graph *g, uint64_t *sum, uint64_t *digest, void *stream);
 
 /* Per-kind statistics of the last accx_cn_count: edges[k] owned edges and
  * work[k] probe elements assigned to kind k. */
@@ -264,6 +273,7 @@ typedef struct {
   uint32_t cores, clusters, hubs, outliers; /* PostProcess counts */
   uint64_t similar_entries;                 /* entries with sim = 1 */
   uint64_t noncore_pairs;                   /* unique (cluster, non-core) pairs */
+  uint64_t digest;                          /* order-independent hash of every (vertex, label, cluster) */
 } accx_scan_summary;
 
 /* Runs the SCAN query on the resident counts (accx_cn_count must have run with
@@ -272,6 +282,16 @@ typedef struct {
  * cluster[n] (minimum vertex id of the core's cluster, -1 for non-cores). */
 int accx_scan_query(accx_graph *g, double eps, int mu, uint8_t *sim, int32_t *label, int32_t *cluster,
                     accx_scan_summary *summary, void *stream);
+
+/* Query contexts: the scratch and results of one query.  accx_scan_query uses
+ * the handle's own context; with extra contexts several queries can run on one
+ * resident graph at the same time, each on its own stream (the graph and its
+ * counts are only read).  A context is sized for one graph. */
+typedef struct accx_query_ctx accx_query_ctx;
+int accx_query_ctx_create(const accx_graph *g, accx_query_ctx **out);
+int accx_query_ctx_free(accx_query_ctx *q);
+int accx_scan_query_ctx(const accx_graph *g, accx_query_ctx *q, double eps, int mu, uint8_t *sim, int32_t *label,
+                        int32_t *cluster, accx_scan_summary *summary, void *stream);
 
 /* The sorted unique (cluster id, non-core vertex) pairs of the last query, as
  * pairs[2k] = cluster id, pairs[2k+1] = vertex; cap = capacity in pairs.  Returns
@@ -295,6 +315,61 @@ int accx_similar_exact(uint32_t cnn, uint32_t du, uint32_t dv, double eps);
 /* accx_similar_exact over k triples: out[i] = 0/1. */
 int accx_similar_exact_batch(uint64_t k, const uint32_t *cnn, const uint32_t *du, const uint32_t *dv, double eps,
                              uint8_t *out);
+
+/* ---- request server: continuous batching on one GPU ---------------------------
+ * No reference counterpart (the reference is a single-shot CLI).  The server
+ * keeps a counted graph resident and serves SCAN queries of any (eps, mu) on it,
+ * plus new-graph count requests (a graph generated on the device, counted and
+ * released).  Worker threads, each with its own CUDA stream and query context,
+ * take requests in arrival order, first fit: a request starts as soon as a
+ * worker is free and its estimated device memory fits what is left of the
+ * budget, so requests arriving while others run start at once and overlap on
+ * the GPU.  Every call is thread-safe. */
+#define ACCX_REQ_QUERY 0
+#define ACCX_REQ_COUNT 1
+typedef struct {
+  int type;               /* ACCX_REQ_QUERY or ACCX_REQ_COUNT */
+  double eps;             /* query */
+  int mu;                 /* query */
+  accx_gen_params graph;  /* count: the graph to generate and count */
+} accx_request;
+typedef struct {
+  int status;                 /* ACCX_OK or the failing call's status */
+  int type;
+  double queue_ms, run_ms, latency_ms;  /* submit->start, start->done, submit->done */
+  accx_scan_summary summary;  /* query */
+  uint64_t n, m;              /* count: the graph's size */
+  uint64_t count_sum, count_digest;  /* count: accx_cn_digest of its counts */
+} accx_result;
+typedef struct {
+  int workers;                /* concurrent requests (0 = 4) */
+  uint64_t hbm_budget;        /* bytes requests may hold at once (0 = 64 GiB) */
+  int count_policy;           /* policy for count requests (ACCX_POLICY_*, not TABLE) */
+  int count_sm_percent;       /* SMs count requests may fill, percent (0 = 50); queries keep the rest */
+} accx_server_config;
+typedef struct {
+  uint64_t submitted, completed, failed;
+  double query_p50_ms, query_p99_ms, count_p50_ms, count_p99_ms;
+  double elapsed_s, throughput_rps;
+  int max_concurrent;         /* most requests running at once */
+  uint64_t peak_bytes;        /* most budget bytes held at once */
+} accx_server_stats;
+typedef struct accx_server accx_server;
+
+/* The server reads `resident` (counted already; it is not copied) until destroyed;
+ * creation waits for all work already queued on the device, so a count still
+ * running on any stream is finished before the first request reads it. */
+int accx_server_create(accx_graph *resident, const accx_server_config *cfg, accx_server **out);
+int accx_server_submit(accx_server *s, const accx_request *req, uint64_t *id);
+/* ACCX_ERR_NOT_READY while the request is pending or running. */
+int accx_server_poll(accx_server *s, uint64_t id, accx_result *out);
+/* Waits up to timeout_ms (< 0: no limit) for one request. */
+int accx_server_wait(accx_server *s, uint64_t id, double timeout_ms, accx_result *out);
+int accx_server_drain(accx_server *s);
+int accx_server_stats_get(accx_server *s, accx_server_stats *out);
+/* Device bytes the server would reserve for a request (its admission size). */
+uint64_t accx_server_request_bytes(const accx_server *s, const accx_request *req);
+int accx_server_destroy(accx_server *s);
 
 #ifdef __cplusplus
 }

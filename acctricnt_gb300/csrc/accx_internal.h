@@ -51,6 +51,7 @@ struct accx_graph {
   int32_t *d_dst = nullptr;   // m + ACCX_DST_PAD
   int32_t *d_cnt = nullptr;   // m
   float *d_simkey = nullptr;    // m: similarity key per entry (built by the first query after a count)
+  uint32_t *d_src = nullptr;    // m: source vertex (row) of every entry, built with the keys
   bool key_valid = false;
   uint32_t *d_tilerow = nullptr;   // row of every 256-entry tile's first entry (+1 for the last entry)
   uint32_t *d_rtilerow = nullptr;  // the same for the relabeled CSR

@@ -50,7 +50,8 @@ __device__ __forceinline__ unsigned long long accx_mix64_dev(unsigned long long 
 template <int TILE>
 __global__ void __launch_bounds__(TILE) k_simkey(const uint32_t *__restrict__ off, const uint32_t *__restrict__ tilerow,
                                                  const int32_t *__restrict__ dst, const int32_t *__restrict__ cnt,
-                                                 uint32_t n, uint32_t m, int32_t bias, float *__restrict__ key) {
+                                                 uint32_t n, uint32_t m, int32_t bias, float *__restrict__ key,
+                                                 uint32_t *__restrict__ src) {
   __shared__ accx_tile_rows<TILE> sh;
   uint32_t base = blockIdx.x * (uint32_t)TILE;
   uint32_t e = base + threadIdx.x;
@@ -60,11 +61,12 @@ __global__ void __launch_bounds__(TILE) k_simkey(const uint32_t *__restrict__ of
   const double c = (double)(uint32_t)(cnt[e] - bias + 2);
   const double du = (double)(off[u + 1] - off[u] + 1), dv = (double)(off[v + 1] - off[v] + 1);
   key[e] = (float)(c * c / (du * dv));
+  src[e] = u;
 }
 
 // Similarity bits from the keys: a streaming pass, one 32-bit word per warp.
 __global__ void k_sim_keys(const float *__restrict__ key, const uint32_t *__restrict__ off,
-                           const uint32_t *__restrict__ tilerow, const int32_t *__restrict__ dst,
+                           const uint32_t *__restrict__ src, const int32_t *__restrict__ dst,
                            const int32_t *__restrict__ cnt, uint32_t n, uint32_t m, int32_t bias, accx_simq q,
                            float lo, float hi, uint32_t *__restrict__ simbits, unsigned long long *__restrict__ qc) {
   const uint32_t stride = gridDim.x * blockDim.x;  // a multiple of 32
@@ -78,9 +80,9 @@ __global__ void k_sim_keys(const float *__restrict__ key, const uint32_t *__rest
         const float k = __ldg(key + e);
         if (k > hi) sim = true;
         else if (k >= lo) {
-          // ambiguous band: exact test with the entry's own numbers
-          const uint32_t t = e >> 8;
-          const uint32_t u = accx_row_of(off, __ldg(tilerow + t), __ldg(tilerow + t + 1) + 1, e);
+          // ambiguous band (exact ties x == eps land here): exact test with the
+          // entry's own numbers
+          const uint32_t u = __ldg(src + e);
           const uint32_t v = (uint32_t)dst[e];
           sim = accx_similar(q, (uint32_t)(cnt[e] - bias + 2), off[u + 1] - off[u] + 1, off[v + 1] - off[v] + 1);
         }
@@ -193,8 +195,8 @@ __device__ __forceinline__ int32_t uf_find(volatile int32_t *parent, int32_t x) 
 // Union over similar core-core entries: one thread per similarity word, only
 // set bits do work.  UnionThreadSafe (union_find.h:22-35): hook the larger root
 // under the smaller.
-__global__ void k_hook_words(const uint32_t *__restrict__ off, const uint32_t *__restrict__ tilerow,
-                             const int32_t *__restrict__ dst, uint32_t m, const uint32_t *__restrict__ simbits,
+__global__ void k_hook_words(const uint32_t *__restrict__ src, const int32_t *__restrict__ dst, uint32_t m,
+                             const uint32_t *__restrict__ simbits,
                              const uint32_t *__restrict__ corebits, int32_t *parent) {
   volatile int32_t *vp = parent;
   const uint32_t words = (m + 31) / 32;
@@ -205,8 +207,7 @@ __global__ void k_hook_words(const uint32_t *__restrict__ off, const uint32_t *_
       w &= w - 1;
       const uint32_t v = (uint32_t)dst[e];
       if (!accx_is_core(corebits, v)) continue;
-      const uint32_t t = e >> 8;
-      const uint32_t u = accx_row_of(off, __ldg(tilerow + t), __ldg(tilerow + t + 1) + 1, e);
+      const uint32_t u = __ldg(src + e);
       if (u >= v || !accx_is_core(corebits, u)) continue;
       for (;;) {
         int32_t ru = uf_find(vp, (int32_t)u), rv = uf_find(vp, (int32_t)v);
@@ -240,14 +241,36 @@ __global__ void k_hub_push(const uint32_t *__restrict__ off, const int32_t *__re
     while (cw) {
       const uint32_t v = wi * 32u + (uint32_t)(__ffs(cw) - 1);
       cw &= cw - 1;
-      const int32_t r = parent[v];
       const uint32_t b = off[v], e = off[v + 1];
+      if (e - b > BIG_ROW) continue;  // k_hub_push_big spreads long rows over many CTAs
+      const int32_t r = parent[v];
       for (uint32_t j = b + lane; j < e; j += 32) {
         const uint32_t u = (uint32_t)dst[j];
         if (accx_is_core(corebits, u)) continue;
         atomicMin(&hubmin[u], r);
         atomicMax(&hubmax[u], r);
       }
+    }
+  }
+}
+
+// The long core rows (the big list of k_cores): blockIdx.y walks the list,
+// blockIdx.x and the threads split each row.
+__global__ void k_hub_push_big(const uint32_t *__restrict__ off, const int32_t *__restrict__ dst,
+                               const uint32_t *__restrict__ big, const unsigned long long *__restrict__ qc,
+                               const uint32_t *__restrict__ corebits, const int32_t *__restrict__ parent,
+                               int32_t *__restrict__ hubmin, int32_t *__restrict__ hubmax) {
+  const unsigned long long nb = qc[Q_BIG];
+  for (unsigned long long i = blockIdx.y; i < nb; i += gridDim.y) {
+    const uint32_t v = big[i];
+    if (!accx_is_core(corebits, v)) continue;
+    const int32_t r = parent[v];
+    const uint32_t b = off[v], e = off[v + 1];
+    for (uint32_t j = b + blockIdx.x * blockDim.x + threadIdx.x; j < e; j += gridDim.x * blockDim.x) {
+      const uint32_t u = (uint32_t)dst[j];
+      if (accx_is_core(corebits, u)) continue;
+      atomicMin(&hubmin[u], r);
+      atomicMax(&hubmax[u], r);
     }
   }
 }
@@ -370,9 +393,11 @@ extern "C" int accx_scan_query_ctx(const accx_graph *g, accx_query_ctx *q, doubl
       accx_graph *gm = const_cast<accx_graph *>(g);
       if (!gm->d_simkey) {
         ACCX_CUDA_TRY(accx_dev_alloc((void **)&gm->d_simkey, sizeof(float) * (size_t)m, g->home));
+        ACCX_CUDA_TRY(accx_dev_alloc((void **)&gm->d_src, sizeof(uint32_t) * (size_t)m, g->home));
         if (g->home) ACCX_CUDA_TRY(cudaStreamSynchronize(g->home));
       }
-      k_simkey<256><<<tiles, 256, 0, s>>>(g->d_off, g->d_tilerow, g->d_dst, g->d_cnt, n, m, g->cnt_bias, gm->d_simkey);
+      k_simkey<256><<<tiles, 256, 0, s>>>(g->d_off, g->d_tilerow, g->d_dst, g->d_cnt, n, m, g->cnt_bias, gm->d_simkey,
+                                          gm->d_src);
       ACCX_CUDA_TRY(cudaStreamSynchronize(s));
       gm->key_valid = true;
     }
@@ -380,7 +405,7 @@ extern "C" int accx_scan_query_ctx(const accx_graph *g, accx_query_ctx *q, doubl
   // threshold band on the keys: exact outside, simpred.h inside
   const float klo = sq.mode == 0 ? (float)sq.m2_lo * (1.0f - 4e-7f) : 0.f;
   const float khi = sq.mode == 0 ? (float)sq.m2_hi * (1.0f + 4e-7f) : 0.f;
-  if (m) k_sim_keys<<<sms * 8, 256, 0, s>>>(g->d_simkey, g->d_off, g->d_tilerow, g->d_dst, g->d_cnt, n, m, g->cnt_bias,
+  if (m) k_sim_keys<<<sms * 8, 256, 0, s>>>(g->d_simkey, g->d_off, g->d_src, g->d_dst, g->d_cnt, n, m, g->cnt_bias,
                                             sq, klo, khi, q->d_simbits, q->d_qcounters);
   if (n) {
     k_cores<<<sms * 8, 256, 0, s>>>(g->d_off, n, mu, q->d_simbits, q->d_core_count, q->d_label, q->d_parent,
@@ -388,11 +413,13 @@ extern "C" int accx_scan_query_ctx(const accx_graph *g, accx_query_ctx *q, doubl
     k_cores_big<<<sms * 2, 256, 0, s>>>(g->d_off, mu, q->d_simbits, q->d_big, q->d_qcounters, q->d_core_count,
                                         q->d_label, q->d_corebits);
   }
-  if (m) k_hook_words<<<sms * 8, 256, 0, s>>>(g->d_off, g->d_tilerow, g->d_dst, m, q->d_simbits, q->d_corebits,
-                                              q->d_parent);
+  if (m) k_hook_words<<<sms * 8, 256, 0, s>>>(g->d_src, g->d_dst, m, q->d_simbits, q->d_corebits, q->d_parent);
   if (n) k_compress<<<sms * 4, 256, 0, s>>>(n, q->d_corebits, q->d_parent);
-  if (n) k_hub_push<<<sms * 8, 256, 0, s>>>(g->d_off, g->d_dst, n, q->d_corebits, q->d_parent, q->d_hubmin,
-                                            q->d_hubmax);
+  if (n) {
+    k_hub_push<<<sms * 8, 256, 0, s>>>(g->d_off, g->d_dst, n, q->d_corebits, q->d_parent, q->d_hubmin, q->d_hubmax);
+    k_hub_push_big<<<dim3(16, 64), 256, 0, s>>>(g->d_off, g->d_dst, q->d_big, q->d_qcounters, q->d_corebits,
+                                                 q->d_parent, q->d_hubmin, q->d_hubmax);
+  }
   bool cl_dev = cluster && accx_is_device_ptr(cluster);
   int32_t *cl_target = cl_dev ? cluster : nullptr;
   if (n) k_finish<<<sms * 4, 256, 0, s>>>(n, q->d_label, q->d_parent, q->d_hubmin, q->d_hubmax, cl_target, q->d_qcounters);

@@ -133,6 +133,11 @@ def _load():
         "accx_graph_set_model": (C.c_int, [P, P]),
         "accx_batch_create": (C.c_int, [P, C.c_int, P, C.POINTER(P)]),
         "accx_cn_digest": (C.c_int, [P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), P]),
+        "accx_graph_from_edges": (C.c_int, [P, P, C.c_uint64, C.c_uint32, P, C.POINTER(P)]),
+        "accx_triangles": (C.c_int, [P, C.POINTER(C.c_uint64), P]),
+        "accx_cn_save": (C.c_int, [P, C.c_char_p]),
+        "accx_cn_load": (C.c_int, [P, C.c_char_p]),
+        "accx_vertex_ranges": (C.c_int, [P, C.c_int, P, P]),
         "accx_query_ctx_create": (C.c_int, [P, C.POINTER(P)]),
         "accx_query_ctx_free": (C.c_int, [P]),
         "accx_server_create": (C.c_int, [P, C.POINTER(ServerConfig), C.POINTER(P)]),
@@ -285,6 +290,16 @@ class Graph:
         return cls(h)
 
     @classmethod
+    def from_edges(cls, src, dst, n, stream=None):
+        """Graph from an undirected edge list (the converter's job, on the device)."""
+        src = np.ascontiguousarray(src, np.uint32)
+        dst = np.ascontiguousarray(dst, np.uint32)
+        h = C.c_void_p()
+        _check(lib.accx_graph_from_edges(_ptr(src), _ptr(dst), len(src), int(n), _stream_ptr(stream), C.byref(h)),
+               "graph_from_edges")
+        return cls(h)
+
+    @classmethod
     def generate(cls, params, stream=None):
         h = C.c_void_p()
         _check(lib.accx_graph_generate(C.byref(params), _stream_ptr(stream), C.byref(h)), "graph_generate")
@@ -353,6 +368,22 @@ class Graph:
         a, b = C.c_uint64(), C.c_uint64()
         _check(lib.accx_cn_digest(self._h, C.byref(a), C.byref(b), _stream_ptr(stream)), "cn_digest")
         return int(a.value), int(b.value)
+
+    def triangles(self, stream=None):
+        t = C.c_uint64()
+        _check(lib.accx_triangles(self._h, C.byref(t), _stream_ptr(stream)), "triangles")
+        return int(t.value)
+
+    def save_counts(self, path):
+        _check(lib.accx_cn_save(self._h, path.encode()), "cn_save")
+
+    def load_counts(self, path):
+        _check(lib.accx_cn_load(self._h, path.encode()), "cn_load")
+
+    def vertex_ranges(self, parts, stream=None):
+        r = np.zeros(parts + 1, np.uint32)
+        _check(lib.accx_vertex_ranges(self._h, int(parts), _ptr(r), _stream_ptr(stream)), "vertex_ranges")
+        return r
 
     def read_counts(self, stream=None):
         """The resident counts (after a count or a captured replay), to the host."""

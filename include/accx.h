@@ -112,6 +112,32 @@ int accx_graph_generate(const accx_gen_params *params, void *stream, accx_graph 
  * with off/dst NULL it returns the sizes; then fill caller buffers of n+1 / m. */
 int accx_generate_host(const accx_gen_params *params, uint32_t *n, uint64_t *m, uint32_t *off, int32_t *dst);
 
+/* Builds a graph from an undirected edge list on the device, as the
+ * reference's EdgeListToBinsConverter does on the host
+ * (scan-query/converter/EdgeListToBinsConverter.cpp:24-126): both directions of
+ * every (src[i], dst[i]) are kept, self loops and duplicates dropped, lists
+ * sorted.  n = number of vertices (ids must be < n); src/dst host or device. */
+int accx_graph_from_edges(const uint32_t *src, const uint32_t *dst, uint64_t k, uint32_t n, void *stream,
+                          accx_graph **out);
+
+/* Triangles of the graph from its resident counts: sum of all counts / 6
+ * (every triangle adds one common neighbour to each of its 3 edges, both
+ * directions).  Needs a count (any bias; the bias is removed). */
+int accx_triangles(const accx_graph *g, uint64_t *triangles, void *stream);
+
+/* Count persistence: writes the resident counts (int32 per entry, the bias
+ * included) with a header of n, m and bias to `path`, and reads them back into
+ * a handle of the same graph, so a restarted server need not recount. */
+int accx_cn_save(const accx_graph *g, const char *path);
+int accx_cn_load(accx_graph *g, const char *path);
+
+/* Splits [0, n) into `parts` vertex ranges of equal filtered cost, cost(u) =
+ * sum over v in N(u), v > u of (deg v + 2) -- the reference's multi-GPU
+ * partitioner ComputeVertexRangeAccumulatedFilteredDegree
+ * (scan-query-cuda/scan_xp_multi_gpu_multi_pass_common.cu:516-554), computed on
+ * the device.  ranges[parts+1]: ranges[0] = 0, ranges[parts] = n. */
+int accx_vertex_ranges(const accx_graph *g, int parts, uint32_t *ranges, void *stream);
+
 /* Writes a CSR in the reference's b_degree.bin / b_adj.bin format. */
 int accx_write_graph_dir(const char *dir, const uint32_t *off, const int32_t *dst, uint32_t n, uint64_t m);
 

@@ -338,3 +338,33 @@ int64_t oracle_cn_count_owners(uint32_t n, const uint32_t *off, const int32_t *d
   }
   return done;
 }
+
+/* ComputeVertexRangeAccumulatedFilteredDegree
+ * (scan-query-cuda/scan_xp_multi_gpu_multi_pass_common.cu:516-554): cost(u) =
+ * sum over v in N(u), v >= u (lower_bound of u in N(u)) of (deg v + 2); the
+ * exclusive prefix over vertices is cut at total/parts*i by lower_bound.  The
+ * per-vertex cost is kept in 64 bits (the reference's uint32 can wrap for hubs). */
+void oracle_vertex_ranges(uint32_t n, const uint32_t *off, const int32_t *dst, int parts, uint32_t *ranges) {
+  uint64_t *prefix = (uint64_t *)malloc(sizeof(uint64_t) * ((size_t)n + 1));
+  prefix[0] = 0;
+  for (uint32_t u = 0; u < n; u++) {
+    uint64_t c = 0;
+    for (uint32_t j = off[u]; j < off[u + 1]; j++) {
+      uint32_t v = (uint32_t)dst[j];
+      if (v >= u) c += off[v + 1] - off[v] + 2;
+    }
+    prefix[u + 1] = prefix[u] + c;
+  }
+  ranges[0] = 0;
+  for (int i = 1; i < parts; i++) {
+    uint64_t target = prefix[n] / (uint64_t)parts * (uint64_t)i;
+    uint32_t lo = 0, hi = n + 1; /* first index with prefix >= target */
+    while (lo < hi) {
+      uint32_t mid = lo + (hi - lo) / 2;
+      if (prefix[mid] < target) lo = mid + 1; else hi = mid;
+    }
+    ranges[i] = lo;
+  }
+  ranges[parts] = n;
+  free(prefix);
+}

@@ -45,6 +45,8 @@ def _load():
     lib.oracle_eps_string.argtypes = [C.c_double, C.c_char_p, C.c_int]
     lib.oracle_cn_count_owners.restype = C.c_int64
     lib.oracle_cn_count_owners.argtypes = [C.c_uint32, P, P, P, C.c_int64, C.c_int, P]
+    lib.oracle_vertex_ranges.restype = None
+    lib.oracle_vertex_ranges.argtypes = [C.c_uint32, P, P, C.c_int, P]
     lib.oracle_sim_batch.restype = None
     lib.oracle_sim_batch.argtypes = [C.c_int64, P, P, P, C.c_double, P]
     return lib
@@ -145,6 +147,13 @@ def sim_batch(cnn, du, dv, eps):
     out = np.zeros(max(len(cnn), 1), np.uint8)
     lib.oracle_sim_batch(len(cnn), _p(cnn), _p(du), _p(dv), float(eps), _p(out))
     return out[:len(cnn)].astype(bool)
+
+
+def vertex_ranges(off, dst, parts):
+    off, dst = _csr(off, dst)
+    r = np.zeros(parts + 1, np.uint32)
+    lib.oracle_vertex_ranges(len(off) - 1, _p(off), _p(dst), int(parts), _p(r))
+    return r
 
 
 def eps_string(eps):

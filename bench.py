@@ -314,8 +314,9 @@ def run_gb300(args):
     achieved = ab / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else None
     traffic = None
     try:
-        tr = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
-        traffic = tr.get(dominant)
+        tr = json.load(open(os.path.join(ROOT, "profiles", "traffic.json"))).get(dominant)
+        if tr:  # bytes per probed id measured by ncu on a smaller case, times this launch's probes
+            traffic = int(tr["bytes_per_probe"] * stats[dominant]["work"])
     except Exception:
         pass
     roofline = {"bound": "hbm", "kernel": "k_" + dominant, "achieved": round(achieved, 1) if achieved else None,

@@ -339,6 +339,26 @@ int64_t oracle_cn_count_owners(uint32_t n, const uint32_t *off, const int32_t *d
   return done;
 }
 
+/* Work of every owner in oracle_cn_count_owners, in list elements touched:
+ * 2 d_u (bits set and cleared) + sum over owned v of (d_v + 8) (the probe of N(v)
+ * and the reverse-entry search).  A sample of owners timed with that function
+ * scales to the whole count by total cost / sample cost. */
+void oracle_owner_costs(uint32_t n, const uint32_t *off, const int32_t *dst, int nthreads, uint64_t *cost) {
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 1024)
+#endif
+  for (int64_t i = 0; i < (int64_t)n; i++) {
+    const uint32_t u = (uint32_t)i, du = off[u + 1] - off[u];
+    uint64_t c = 2ull * du;
+    for (uint32_t e = off[u]; e < off[u + 1]; e++) {
+      const uint32_t v = (uint32_t)dst[e], dv = off[v + 1] - off[v];
+      if (du > dv || (du == dv && u < v)) c += (uint64_t)dv + 8u;
+    }
+    cost[u] = c;
+  }
+}
+
 /* ComputeVertexRangeAccumulatedFilteredDegree
  * (scan-query-cuda/scan_xp_multi_gpu_multi_pass_common.cu:516-554): cost(u) =
  * sum over v in N(u), v >= u (lower_bound of u in N(u)) of (deg v + 2); the

@@ -46,6 +46,7 @@ def _load():
     lib.oracle_cn_count_owners.restype = C.c_int64
     lib.oracle_cn_count_owners.argtypes = [C.c_uint32, P, P, P, C.c_int64, C.c_int, P]
     lib.oracle_vertex_ranges.restype = None
+    lib.oracle_owner_costs.argtypes = [C.c_uint32, P, P, C.c_int, P]
     lib.oracle_vertex_ranges.argtypes = [C.c_uint32, P, P, C.c_int, P]
     lib.oracle_sim_batch.restype = None
     lib.oracle_sim_batch.argtypes = [C.c_int64, P, P, P, C.c_double, P]
@@ -88,6 +89,15 @@ def cn_count_owners(off, dst, owners, nthreads=0, cnn=None):
         cnn = np.full(max(len(dst), 1), 2, np.int32)
     k = lib.oracle_cn_count_owners(len(off) - 1, _p(off), _p(dst), _p(owners), len(owners), int(nthreads), _p(cnn))
     return int(k), cnn
+
+
+def owner_costs(off, dst, nthreads=0):
+    """Per-owner work of cn_count_owners (2 d_u + sum over owned v of d_v + 8), uint64[n]."""
+    off, dst = _csr(off, dst)
+    n = len(off) - 1
+    cost = np.zeros(max(n, 1), np.uint64)
+    lib.oracle_owner_costs(n, _p(off), _p(dst), int(nthreads), _p(cost))
+    return cost[:n]
 
 
 def similarity(off, dst, cnn, eps, mu):

@@ -45,7 +45,7 @@ class GenParams(C.Structure):
 class CountOpts(C.Structure):
     _fields_ = [("policy", C.c_int), ("table", C.POINTER(C.c_uint8)), ("bias", C.c_int32),
                 ("block_warps", C.c_int), ("bitmap_window_kb", C.c_int), ("timing", C.c_int), ("sparse_table_kb", C.c_int),
-                ("sm_limit", C.c_int)]
+                ("sm_limit", C.c_int), ("orient", C.c_int)]
 
 
 class ScanSummary(C.Structure):
@@ -131,6 +131,11 @@ def _load():
         "accx_model_predict": (C.c_int, [P, P, C.c_uint32, P]),
         "accx_model_table_for": (C.c_int, [P, P, P]),
         "accx_graph_set_model": (C.c_int, [P, P]),
+        "accx_cn_last_matches": (C.c_int, [P, P, P]),
+        "accx_bucket_stats_oriented": (C.c_int, [P, P, P, P]),
+        "accx_bucket_features_oriented": (C.c_int, [P, P]),
+        "accx_model_table_for_oriented": (C.c_int, [P, P, P]),
+        "accx_graph_set_model_oriented": (C.c_int, [P, P]),
         "accx_batch_create": (C.c_int, [P, C.c_int, P, C.POINTER(P)]),
         "accx_cn_digest": (C.c_int, [P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), P]),
         "accx_graph_from_edges": (C.c_int, [P, P, C.c_uint64, C.c_uint32, P, C.POINTER(P)]),
@@ -336,7 +341,7 @@ class Graph:
         return o.value, d.value, c.value
 
     @staticmethod
-    def _opts(policy, table, bias, block_warps, window_kb, timing=False, sparse_kb=0):
+    def _opts(policy, table, bias, block_warps, window_kb, timing=False, sparse_kb=0, orient=False):
         pol = POLICIES[policy] if isinstance(policy, str) else int(policy)
         tab = None
         keep = None
@@ -344,16 +349,16 @@ class Graph:
             keep = np.ascontiguousarray(table, np.uint8).reshape(-1)
             assert keep.size == NB * NB
             tab = keep.ctypes.data_as(C.POINTER(C.c_uint8))
-            if pol == POLICY_HEURISTIC and isinstance(policy, str) and policy == "heuristic":
-                pass
         return CountOpts(pol, tab, int(bias), int(block_warps), int(window_kb), 1 if timing else 0, int(sparse_kb),
-                         0), keep
+                         0, 1 if orient else 0), keep
 
     def count(self, policy="heuristic", table=None, bias=0, out="host", block_warps=0, window_kb=0, stream=None,
-              timing=False, sparse_kb=0):
+              timing=False, sparse_kb=0, orient=False):
         """All-edge CN counts.  out="host" returns an int32 numpy array; out=None
-        leaves them resident; out=<int device pointer> copies there."""
-        opts, keep = self._opts(policy, table, bias, block_warps, window_kb, timing, sparse_kb)
+        leaves them resident; out=<int device pointer> copies there.  orient=True
+        counts triangles on prefix lists (same result, less work on a relabeled
+        graph); buckets and kinds then refer to prefix lengths."""
+        opts, keep = self._opts(policy, table, bias, block_warps, window_kb, timing, sparse_kb, orient)
         if out == "host":
             res = np.zeros(max(self.m, 1), np.int32)
             _check(lib.accx_cn_count(self._h, C.byref(opts), _ptr(res), _stream_ptr(stream)), "cn_count")
@@ -397,6 +402,13 @@ class Graph:
         _check(lib.accx_cn_last_stats(self._h, _ptr(e), _ptr(w)), "cn_last_stats")
         return {KIND_NAMES[k]: {"edges": int(e[k]), "work": int(w[k])} for k in range(3)}
 
+    def last_matches(self):
+        """Oriented counts: (common ids found per kind, ids probed by the bitmap kind)."""
+        mt = np.zeros(3, np.uint64)
+        pr = C.c_uint64()
+        _check(lib.accx_cn_last_matches(self._h, _ptr(mt), C.byref(pr)), "cn_last_matches")
+        return {KIND_NAMES[k]: int(mt[k]) for k in range(3)}, int(pr.value)
+
     def owner_work(self):
         w = np.zeros(3, np.uint64)
         _check(lib.accx_cn_last_owner_work(self._h, _ptr(w)), "cn_last_owner_work")
@@ -420,21 +432,30 @@ class Graph:
         return ({"block_warps": best.block_warps, "window_kb": best.bitmap_window_kb,
                  "sparse_kb": best.sparse_table_kb}, float(bms.value), allms[:nc.value].tolist())
 
-    def bucket_stats(self):
+    def bucket_stats(self, orient=False):
+        """Per-bucket owned edges and owner / other size sums; orient=True uses
+        prefix lengths on the counting CSR (the oriented buckets)."""
         e = np.zeros(NB * NB, np.uint64)
         so = np.zeros(NB * NB, np.float64)
         sp = np.zeros(NB * NB, np.float64)
-        _check(lib.accx_bucket_stats(self._h, _ptr(e), _ptr(so), _ptr(sp)), "bucket_stats")
+        fn = lib.accx_bucket_stats_oriented if orient else lib.accx_bucket_stats
+        _check(fn(self._h, _ptr(e), _ptr(so), _ptr(sp)), "bucket_stats")
         return e, so, sp
 
-    def bucket_features(self):
+    def bucket_features(self, orient=False):
         x = np.zeros((NB * NB, MODEL_IN), np.float32)
-        _check(lib.accx_bucket_features(self._h, _ptr(x)), "bucket_features")
+        fn = lib.accx_bucket_features_oriented if orient else lib.accx_bucket_features
+        _check(fn(self._h, _ptr(x)), "bucket_features")
         return x
 
-    def set_model(self, model):
-        self._model = model  # keep the model alive while attached
-        _check(lib.accx_graph_set_model(self._h, model._h if model else None), "graph_set_model")
+    def set_model(self, model, orient=False):
+        """Attach the model ACCX_POLICY_MODEL uses (for direct or oriented counts)."""
+        if orient:
+            self._model_or = model  # keep the model alive while attached
+            _check(lib.accx_graph_set_model_oriented(self._h, model._h if model else None), "graph_set_model")
+        else:
+            self._model = model
+            _check(lib.accx_graph_set_model(self._h, model._h if model else None), "graph_set_model")
 
     def scan(self, eps, mu, want_sim=True, want_label=True, want_cluster=True, stream=None):
         sim = np.zeros(max(self.m, 1), np.uint8) if want_sim else None
@@ -508,9 +529,10 @@ class Model:
         _check(lib.accx_model_predict(self._h, _ptr(x), len(x), _ptr(y)), "model_predict")
         return y
 
-    def table_for(self, graph):
+    def table_for(self, graph, orient=False):
         t = np.zeros(NB * NB, np.uint8)
-        _check(lib.accx_model_table_for(self._h, graph._h, _ptr(t)), "model_table_for")
+        fn = lib.accx_model_table_for_oriented if orient else lib.accx_model_table_for
+        _check(fn(self._h, graph._h, _ptr(t)), "model_table_for")
         return t.reshape(NB, NB)
 
 

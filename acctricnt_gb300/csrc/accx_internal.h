@@ -69,6 +69,7 @@ struct accx_graph {
   uint2 *d_edge_list = nullptr;  // m/2+1 owned entries: merge items from the front, gallop from the back
   unsigned long long *d_icnt = nullptr;    // n+1 bitmap items per owner
   unsigned long long *d_prefix = nullptr;  // n+1 exclusive prefix of d_icnt
+  uint32_t *d_pre = nullptr;               // n prefix lengths (neighbours with smaller ids), oriented counts
   void *d_scan_tmp = nullptr;
   size_t scan_tmp_bytes = 0;
   unsigned long long *d_counters = nullptr;  // [0] merge, [1] gallop, [2] bitmap items, [3..5] work per kind
@@ -116,11 +117,15 @@ int accx_sm_count(int device);
 // Internal: creates a handle around device arrays already owned by it.
 int accx_graph_validate_device(accx_graph *g, int full, cudaStream_t s);
 int accx_ensure_count_scratch(accx_graph *g);
+// Prefix lengths (neighbours with smaller ids) of the CSR counts run on (the
+// relabeled copy when there is one) into g->d_pre (count.cu).
+int accx_prefix_lengths(accx_graph *g, cudaStream_t s);
 
-// Cost-model state attached to a handle (model.cu).
+// Cost-model state attached to a handle (model.cu); orient selects the direct
+// (0) or oriented (1) buckets, features and attached model.
 void accx_model_release(accx_graph *g);
 int accx_model_table(accx_graph *g, uint8_t *table);
-int accx_model_table_device(accx_graph *g, cudaStream_t s);
+int accx_model_table_device(accx_graph *g, cudaStream_t s, int orient);
 
 // Exclusive/inclusive helpers implemented in gen.cu.
 // Row index of every 256-entry tile of a CSR (graph.cu), allocated on g's home stream.

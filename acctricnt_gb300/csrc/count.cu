@@ -34,6 +34,8 @@
 #define C_EDGES 3  // + kind
 #define C_WORK 6   // + kind
 #define C_OWNER 9  // + kind: owner-side elements
+#define C_MATCH 12 // + kind: common ids found (oriented counts)
+#define C_PROBED 15 // ids probed by the oriented bitmap kernel
 #define C_NUM 16
 
 #define MERGE_WARPS 8        // warps per merge/gallop CTA
@@ -54,13 +56,18 @@ __device__ __forceinline__ int accx_edge_kind(int policy, const uint8_t *table, 
 }
 
 // ---------------------------------------------------------------------------
-// classify: one thread per CSR entry.
-template <int TILE>
+// classify: one thread per CSR entry.  ORIENT: owners, buckets and kinds use the
+// prefix lengths pre[] in place of degrees; an edge whose smaller prefix is
+// empty closes no triangle from here and is left out; bitmap owners need an id
+// below bm_idlim (their prefix ids fit the dense window) and a prefix of at most
+// bm_pcap ids (the shared counters), otherwise their edges go to merge.
+template <int TILE, bool ORIENT>
 __global__ void __launch_bounds__(TILE) k_classify(const uint32_t *__restrict__ off, const uint32_t *__restrict__ tilerow, const int32_t *__restrict__ dst,
                                                    uint32_t n, uint32_t m, int policy,
                                                    const uint8_t *__restrict__ table, uint2 *__restrict__ list,
                                                    uint32_t list_cap, unsigned long long *__restrict__ work_u,
-                                                   unsigned long long *__restrict__ ctr) {
+                                                   unsigned long long *__restrict__ ctr, const uint32_t *__restrict__ pre,
+                                                   uint32_t bm_idlim, uint32_t bm_pcap) {
   __shared__ accx_tile_rows<TILE> sh;
   __shared__ uint8_t s_table[ACCX_NB * ACCX_NB];
   if (policy == ACCX_POLICY_TABLE || policy == ACCX_POLICY_MODEL)
@@ -72,9 +79,18 @@ __global__ void __launch_bounds__(TILE) k_classify(const uint32_t *__restrict__ 
   uint32_t v = 0, du = 0, dv = 0;
   if (e < m) {
     v = (uint32_t)dst[e];
-    du = off[u + 1] - off[u];
-    dv = off[v + 1] - off[v];
-    if (accx_owns(u, du, v, dv)) kind = accx_edge_kind(policy, s_table, du, dv);
+    if (ORIENT) {
+      du = pre[u];
+      dv = pre[v];
+      if (dv > 0 && accx_owns(u, du, v, dv)) {
+        kind = accx_edge_kind(policy, s_table, du, dv);
+        if (kind == ACCX_KIND_BITMAP && (u >= bm_idlim || du > bm_pcap)) kind = ACCX_KIND_MERGE;
+      }
+    } else {
+      du = off[u + 1] - off[u];
+      dv = off[v + 1] - off[v];
+      if (accx_owns(u, du, v, dv)) kind = accx_edge_kind(policy, s_table, du, dv);
+    }
   }
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
@@ -200,18 +216,19 @@ __device__ __forceinline__ void accx_item_shape(uint32_t du, uint32_t nsp, unsig
 __global__ void k_item_counts(const uint32_t *__restrict__ off, const int32_t *__restrict__ dst, uint32_t n,
                               const unsigned long long *__restrict__ work_u, uint32_t W, uint32_t chs,
                               uint32_t target, unsigned long long *__restrict__ icnt,
-                              unsigned long long *__restrict__ ctr) {
+                              unsigned long long *__restrict__ ctr, const uint32_t *__restrict__ pre) {
   for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u <= n; u += gridDim.x * blockDim.x) {
     unsigned long long c = 0;
     if (u < n) {
       unsigned long long w = work_u[u];
       if (w) {
         uint32_t ub = off[u], ue = off[u + 1];
-        uint32_t us = accx_lower_bound(dst, ub, ue, (int32_t)min(W, 0x7fffffffu));
+        // oriented owners stage only their prefix, all of it in the dense window
+        uint32_t us = pre ? ue : accx_lower_bound(dst, ub, ue, (int32_t)min(W, 0x7fffffffu));
         uint32_t nc, ns;
         accx_item_shape(ue - ub, ue - us, w, chs, target, &nc, &ns);
         c = (unsigned long long)nc * ns;
-        atomicAdd(&ctr[C_OWNER + ACCX_KIND_BITMAP], (unsigned long long)(ue - ub) * ns);
+        atomicAdd(&ctr[C_OWNER + ACCX_KIND_BITMAP], (unsigned long long)(pre ? pre[u] : ue - ub) * ns);
       }
     }
     icnt[u] = c;
@@ -513,6 +530,8 @@ __global__ void __launch_bounds__(1024, 1) k_bitmap(const uint32_t *__restrict__
   }
 }
 
+#include "orient.cuh"
+
 // ---------------------------------------------------------------------------
 // Mirror: each owned entry e=(u,v) adds the bias and copies its count to the
 // reverse entry (the position of u in N(v)).
@@ -543,6 +562,7 @@ int accx_ensure_count_scratch(accx_graph *g) {
   if (!g->d_icnt) {
     ACCX_CUDA_TRY(accx_dev_alloc((void **)&g->d_icnt, sizeof(unsigned long long) * (n + 1), h));
     ACCX_CUDA_TRY(accx_dev_alloc((void **)&g->d_prefix, sizeof(unsigned long long) * (n + 1), h));
+    ACCX_CUDA_TRY(accx_dev_alloc((void **)&g->d_pre, sizeof(uint32_t) * (n ? n : 1), h));
     size_t bytes = 0;
     ACCX_CUDA_TRY(cub::DeviceScan::ExclusiveSum(nullptr, bytes, g->d_icnt, g->d_prefix, (int64_t)n + 1));
     ACCX_CUDA_TRY(accx_dev_alloc(&g->d_scan_tmp, bytes ? bytes : 16, h));
@@ -560,21 +580,37 @@ int accx_ensure_count_scratch(accx_graph *g) {
   return ACCX_OK;
 }
 
-// Tuned defaults (overridable per call).
+int accx_prefix_lengths(accx_graph *g, cudaStream_t s) {
+  int rc = accx_ensure_count_scratch(g);
+  if (rc) return rc;
+  const bool rel = g->d_roff != nullptr;
+  if (g->n) k_pre<<<accx_sm_count(g->device) * 8, 256, 0, s>>>(rel ? g->d_roff : g->d_off, rel ? g->d_rdst : g->d_dst,
+                                                                g->n, g->d_pre);
+  ACCX_CUDA_TRY(cudaGetLastError());
+  return ACCX_OK;
+}
+
+// Tuned defaults (overridable per call).  Oriented counts read bitmap_window_kb
+// as the dense window and sparse_table_kb as the owner-prefix counters.
 static int g_block_warps = 32;
 static int g_dense_kb = 128;
 static int g_sparse_kb = 64;
+static int g_or_dense_kb = 96;
+static int g_or_counter_kb = 16;
 
 
 static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s) {
   const uint32_t n = g->n, m = (uint32_t)g->m;
   int policy = o ? o->policy : ACCX_POLICY_HEURISTIC;
   int32_t bias = o ? o->bias : 0;
+  const bool orient = o && o->orient;
   int warps = (o && o->block_warps > 0) ? o->block_warps : g_block_warps;
-  int dkb = (o && o->bitmap_window_kb > 0) ? o->bitmap_window_kb : g_dense_kb;
-  int skb = (o && o->sparse_table_kb > 0) ? o->sparse_table_kb : g_sparse_kb;
+  int dkb = (o && o->bitmap_window_kb > 0) ? o->bitmap_window_kb : (orient ? g_or_dense_kb : g_dense_kb);
+  int skb = (o && o->sparse_table_kb > 0) ? o->sparse_table_kb : (orient ? g_or_counter_kb : g_sparse_kb);
   if (policy < ACCX_POLICY_HEURISTIC || policy > ACCX_POLICY_MODEL) return ACCX_ERR_INVALID_ARG;
-  if (warps < 1 || warps > 32 || dkb < 1 || skb < 1 || dkb + skb > 200) return ACCX_ERR_INVALID_ARG;
+  if (o && (o->orient < 0 || o->orient > 1)) return ACCX_ERR_INVALID_ARG;
+  if (warps < 1 || warps > 32 || dkb < 1 || skb < 1) return ACCX_ERR_INVALID_ARG;
+  if (orient ? (dkb + dkb / 2 + skb > 196 || skb > 200) : (dkb + skb > 200)) return ACCX_ERR_INVALID_ARG;
   if (n == 0) {
     g->cnt_bias = bias;
     g->cnt_valid = true;
@@ -589,7 +625,7 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s)
     ACCX_CUDA_TRY(cudaMemcpyAsync(g->d_table, o->table, ACCX_NB * ACCX_NB, cudaMemcpyHostToDevice, s));
     ACCX_CUDA_TRY(cudaStreamSynchronize(s));  // o->table is pageable caller memory
   } else if (policy == ACCX_POLICY_MODEL) {
-    rc = accx_model_table_device(g, s);  // the attached model writes g->d_table on the device
+    rc = accx_model_table_device(g, s, orient ? 1 : 0);  // the attached model writes g->d_table on the device
     if (rc) return rc;
   }
   // counting runs on the relabeled CSR when the handle has one
@@ -616,29 +652,56 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s)
 #define ACCX_MARK(i) \
   if (timing) ACCX_CUDA_TRY(cudaEventRecord(g->ev[i], s));
   ACCX_MARK(0);
-  k_classify<256><<<tiles, 256, 0, s>>>(off, tilerow, dst, n, m, policy, g->d_table, g->d_edge_list, list_cap, work_u, ctr);
   int sms = accx_sm_count(g->device);
   if (o && o->sm_limit > 0 && o->sm_limit < sms) sms = o->sm_limit;
-  const uint32_t W = (uint32_t)dkb * 8192u;        // dense ids (bits)
-  const uint32_t S = (uint32_t)skb * 1024u / 8u;   // sparse 8-byte slots
-  const size_t smem = (size_t)W / 8u + (size_t)S * 8u;
-  const uint32_t target = ITEM_TARGET_DEFAULT;
-  k_item_counts<<<sms * 4, 256, 0, s>>>(off, dst, n, work_u, W, S / 2, target, g->d_icnt, ctr);
-  ACCX_CUDA_TRY(cub::DeviceScan::ExclusiveSum(g->d_scan_tmp, g->scan_tmp_bytes, g->d_icnt, g->d_prefix,
-                                              (int64_t)n + 1, s));
-  ACCX_MARK(1);
-  k_merge<<<sms * 8, MERGE_WARPS * 32, 0, s>>>(off, dst, g->d_edge_list, list_cap, ctr, cnt);
-  ACCX_MARK(2);
-  k_gallop<<<sms * 8, MERGE_WARPS * 32, 0, s>>>(off, dst, g->d_edge_list, list_cap, ctr, cnt);
-  ACCX_MARK(3);
-  ACCX_CUDA_TRY(cudaFuncSetAttribute(k_bitmap, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int per_sm = 0;
-  ACCX_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bitmap, warps * 32, smem));
-  if (per_sm < 1) return ACCX_ERR_INVALID_ARG;
-  k_bitmap<<<sms * per_sm, warps * 32, smem, s>>>(off, dst, n, policy, g->d_table, work_u, g->d_prefix, W, S, target,
-                                                  cnt);
-  ACCX_MARK(4);
-  k_mirror<256><<<tiles, 256, 0, s>>>(off, tilerow, dst, n, m, bias, cnt);
+  if (orient) {
+    const uint32_t W = (uint32_t)dkb * 8192u;       // dense ids (bits); bitmap owners have ids below W
+    const uint32_t pcap = (uint32_t)skb * 256u;     // owner-prefix counters
+    const size_t smem = (size_t)W / 8u + (size_t)pcap * 4u + (size_t)W / 16u;
+    const uint32_t target = ITEM_TARGET_DEFAULT;
+    k_pre<<<sms * 8, 256, 0, s>>>(off, dst, n, g->d_pre);
+    k_classify<256, true><<<tiles, 256, 0, s>>>(off, tilerow, dst, n, m, policy, g->d_table, g->d_edge_list, list_cap,
+                                                work_u, ctr, g->d_pre, W, pcap);
+    k_item_counts<<<sms * 4, 256, 0, s>>>(off, dst, n, work_u, W, 1, target, g->d_icnt, ctr, g->d_pre);
+    ACCX_CUDA_TRY(cub::DeviceScan::ExclusiveSum(g->d_scan_tmp, g->scan_tmp_bytes, g->d_icnt, g->d_prefix,
+                                                (int64_t)n + 1, s));
+    ACCX_MARK(1);
+    k_merge_or<<<sms * 8, MERGE_WARPS * 32, 0, s>>>(off, dst, g->d_pre, g->d_edge_list, list_cap, ctr, cnt);
+    ACCX_MARK(2);
+    k_gallop_or<<<sms * 8, MERGE_WARPS * 32, 0, s>>>(off, dst, g->d_pre, g->d_edge_list, list_cap, ctr, cnt);
+    ACCX_MARK(3);
+    ACCX_CUDA_TRY(cudaFuncSetAttribute(k_bitmap_or, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    ACCX_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bitmap_or, warps * 32, smem));
+    if (per_sm < 1) return ACCX_ERR_INVALID_ARG;
+    k_bitmap_or<<<sms * per_sm, warps * 32, smem, s>>>(off, dst, g->d_pre, n, policy, g->d_table, work_u, g->d_prefix,
+                                                       W, pcap, target, cnt, ctr);
+    ACCX_MARK(4);
+    k_combine_or<256><<<tiles, 256, 0, s>>>(off, tilerow, dst, g->d_pre, n, m, bias, cnt);
+  } else {
+    k_classify<256, false><<<tiles, 256, 0, s>>>(off, tilerow, dst, n, m, policy, g->d_table, g->d_edge_list, list_cap,
+                                                 work_u, ctr, nullptr, 0u, 0u);
+    const uint32_t W = (uint32_t)dkb * 8192u;        // dense ids (bits)
+    const uint32_t S = (uint32_t)skb * 1024u / 8u;   // sparse 8-byte slots
+    const size_t smem = (size_t)W / 8u + (size_t)S * 8u;
+    const uint32_t target = ITEM_TARGET_DEFAULT;
+    k_item_counts<<<sms * 4, 256, 0, s>>>(off, dst, n, work_u, W, S / 2, target, g->d_icnt, ctr, nullptr);
+    ACCX_CUDA_TRY(cub::DeviceScan::ExclusiveSum(g->d_scan_tmp, g->scan_tmp_bytes, g->d_icnt, g->d_prefix,
+                                                (int64_t)n + 1, s));
+    ACCX_MARK(1);
+    k_merge<<<sms * 8, MERGE_WARPS * 32, 0, s>>>(off, dst, g->d_edge_list, list_cap, ctr, cnt);
+    ACCX_MARK(2);
+    k_gallop<<<sms * 8, MERGE_WARPS * 32, 0, s>>>(off, dst, g->d_edge_list, list_cap, ctr, cnt);
+    ACCX_MARK(3);
+    ACCX_CUDA_TRY(cudaFuncSetAttribute(k_bitmap, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    ACCX_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bitmap, warps * 32, smem));
+    if (per_sm < 1) return ACCX_ERR_INVALID_ARG;
+    k_bitmap<<<sms * per_sm, warps * 32, smem, s>>>(off, dst, n, policy, g->d_table, work_u, g->d_prefix, W, S, target,
+                                                    cnt);
+    ACCX_MARK(4);
+    k_mirror<256><<<tiles, 256, 0, s>>>(off, tilerow, dst, n, m, bias, cnt);
+  }
   if (rel) {
     rc = accx_relabel_gather(g, s);
     if (rc) return rc;
@@ -688,6 +751,17 @@ extern "C" int accx_cn_last_owner_work(const accx_graph *g, uint64_t owner_work[
   ACCX_CUDA_TRY(cudaDeviceSynchronize());
   ACCX_CUDA_TRY(cudaMemcpy(h, g->d_counters, sizeof(h), cudaMemcpyDeviceToHost));
   for (int k = 0; k < ACCX_NUM_KINDS; k++) owner_work[k] = h[C_OWNER + k];
+  return ACCX_OK;
+}
+
+extern "C" int accx_cn_last_matches(const accx_graph *g, uint64_t matches[ACCX_NUM_KINDS], uint64_t *probed) {
+  if (!g || !g->d_counters) return ACCX_ERR_INVALID_ARG;
+  unsigned long long h[C_NUM];
+  ACCX_CUDA_TRY(cudaDeviceSynchronize());
+  ACCX_CUDA_TRY(cudaMemcpy(h, g->d_counters, sizeof(h), cudaMemcpyDeviceToHost));
+  for (int k = 0; k < ACCX_NUM_KINDS; k++)
+    if (matches) matches[k] = h[C_MATCH + k];
+  if (probed) *probed = h[C_PROBED];
   return ACCX_OK;
 }
 

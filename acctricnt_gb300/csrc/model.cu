@@ -194,9 +194,12 @@ __global__ void __launch_bounds__(256) k_model_infer(const __half *__restrict__ 
 // ---------------------------------------------------------------------------
 // Bucket statistics over owned edges: per block shared histograms, then global.
 #define NBB (ACCX_NB * ACCX_NB)
-template <int TILE>
+// ORIENT: owners and buckets by prefix length (pre), edges whose smaller prefix is
+// empty left out -- the edges and sizes oriented counting works on.
+template <int TILE, bool ORIENT>
 __global__ void __launch_bounds__(TILE) k_bucket_stats(const uint32_t *__restrict__ off, const uint32_t *__restrict__ tilerow, const int32_t *__restrict__ dst,
-                                                       uint32_t n, uint32_t m, unsigned long long *__restrict__ st) {
+                                                       uint32_t n, uint32_t m, unsigned long long *__restrict__ st,
+                                                       const uint32_t *__restrict__ pre) {
   __shared__ accx_tile_rows<TILE> sh;
   __shared__ unsigned long long hs[3 * NBB];
   for (int i = threadIdx.x; i < 3 * NBB; i += TILE) hs[i] = 0;
@@ -205,8 +208,15 @@ __global__ void __launch_bounds__(TILE) k_bucket_stats(const uint32_t *__restric
   uint32_t u = accx_tile_row<TILE>(off, tilerow, n, m, base, e, &sh);  // contains __syncthreads
   if (e < m) {
     uint32_t v = (uint32_t)dst[e];
-    uint32_t du = off[u + 1] - off[u], dv = off[v + 1] - off[v];
-    if (accx_owns(u, du, v, dv)) {
+    uint32_t du, dv;
+    if (ORIENT) {
+      du = pre[u];
+      dv = pre[v];
+    } else {
+      du = off[u + 1] - off[u];
+      dv = off[v + 1] - off[v];
+    }
+    if ((!ORIENT || dv > 0) && accx_owns(u, du, v, dv)) {
       int b = accx_bucket(du) * ACCX_NB + accx_bucket(dv);
       atomicAdd(&hs[b], 1ull);
       atomicAdd(&hs[NBB + b], (unsigned long long)du);
@@ -243,10 +253,13 @@ __global__ void k_features(const unsigned long long *__restrict__ st, uint32_t n
 // Per-handle cache: bucket statistics and features of the graph (it never
 // changes), plus the attached model.
 struct accx_graph_model_state {
-  unsigned long long *d_stats = nullptr;  // 3 * NBB
-  float *d_feat = nullptr;                // NBB * IN
-  bool ready = false;
-  accx_model *model = nullptr;
+  // [0] direct: degrees on the handle's CSR; [1] oriented: prefix lengths on the
+  // CSR counts run on (recomputed when that changes, i.e. after a relabel)
+  unsigned long long *d_stats[2] = {nullptr, nullptr};  // 3 * NBB each
+  float *d_feat[2] = {nullptr, nullptr};                // NBB * IN each
+  bool ready[2] = {false, false};
+  const uint32_t *csr[2] = {nullptr, nullptr};
+  accx_model *model[2] = {nullptr, nullptr};
 };
 
 static accx_graph_model_state *state_of(accx_graph *g) {
@@ -257,35 +270,50 @@ static accx_graph_model_state *state_of(accx_graph *g) {
 void accx_model_release(accx_graph *g) {
   auto *st = static_cast<accx_graph_model_state *>(g->model);
   if (st) {
-    if (st->d_stats) cudaFree(st->d_stats);
-    if (st->d_feat) cudaFree(st->d_feat);
+    for (int i = 0; i < 2; i++) {
+      if (st->d_stats[i]) cudaFree(st->d_stats[i]);
+      if (st->d_feat[i]) cudaFree(st->d_feat[i]);
+    }
     delete st;
   }
   g->model = nullptr;
 }
 
-static int ensure_features(accx_graph *g, cudaStream_t s) {
+static int ensure_features(accx_graph *g, cudaStream_t s, int mode) {
   accx_graph_model_state *st = state_of(g);
   if (!st) return ACCX_ERR_OOM;
-  if (st->ready) return ACCX_OK;
-  if (!st->d_stats) ACCX_CUDA_TRY(cudaMalloc(&st->d_stats, sizeof(unsigned long long) * 3 * NBB));
-  if (!st->d_feat) ACCX_CUDA_TRY(cudaMalloc(&st->d_feat, sizeof(float) * NBB * IN));
-  ACCX_CUDA_TRY(cudaMemsetAsync(st->d_stats, 0, sizeof(unsigned long long) * 3 * NBB, s));
+  const bool rel = mode == 1 && g->d_roff != nullptr;
+  const uint32_t *off = rel ? g->d_roff : g->d_off;
+  if (st->ready[mode] && st->csr[mode] == off) return ACCX_OK;
+  if (!st->d_stats[mode]) ACCX_CUDA_TRY(cudaMalloc(&st->d_stats[mode], sizeof(unsigned long long) * 3 * NBB));
+  if (!st->d_feat[mode]) ACCX_CUDA_TRY(cudaMalloc(&st->d_feat[mode], sizeof(float) * NBB * IN));
+  ACCX_CUDA_TRY(cudaMemsetAsync(st->d_stats[mode], 0, sizeof(unsigned long long) * 3 * NBB, s));
   const uint32_t m = (uint32_t)g->m;
-  if (m) k_bucket_stats<256><<<(m + 255) / 256, 256, 0, s>>>(g->d_off, g->d_tilerow, g->d_dst, g->n, m, st->d_stats);
-  k_features<<<(NBB + 127) / 128, 128, 0, s>>>(st->d_stats, g->n, g->m, st->d_feat);
+  if (mode == 0) {
+    if (m) k_bucket_stats<256, false><<<(m + 255) / 256, 256, 0, s>>>(g->d_off, g->d_tilerow, g->d_dst, g->n, m,
+                                                                    st->d_stats[0], nullptr);
+  } else if (m) {
+    int rc = accx_prefix_lengths(g, s);
+    if (rc) return rc;
+    k_bucket_stats<256, true><<<(m + 255) / 256, 256, 0, s>>>(off, rel ? g->d_rtilerow : g->d_tilerow,
+                                                             rel ? g->d_rdst : g->d_dst, g->n, m, st->d_stats[1],
+                                                             g->d_pre);
+  }
+  k_features<<<(NBB + 127) / 128, 128, 0, s>>>(st->d_stats[mode], g->n, g->m, st->d_feat[mode]);
   ACCX_CUDA_TRY(cudaGetLastError());
-  st->ready = true;
+  st->ready[mode] = true;
+  st->csr[mode] = off;
   return ACCX_OK;
 }
 
 // The handle's ACCX_POLICY_MODEL table, computed on the device into g->d_table.
-int accx_model_table_device(accx_graph *g, cudaStream_t s) {
+int accx_model_table_device(accx_graph *g, cudaStream_t s, int orient) {
   accx_graph_model_state *st = state_of(g);
-  if (!st || !st->model) return ACCX_ERR_NOT_READY;
-  int rc = ensure_features(g, s);
+  const int mode = orient ? 1 : 0;
+  if (!st || !st->model[mode]) return ACCX_ERR_NOT_READY;
+  int rc = ensure_features(g, s, mode);
   if (rc) return rc;
-  k_model_infer<<<8, 256, 0, s>>>(st->model->d_w, st->d_feat, NBB, nullptr, st->d_stats, g->d_table);
+  k_model_infer<<<8, 256, 0, s>>>(st->model[mode]->d_w, st->d_feat[mode], NBB, nullptr, st->d_stats[mode], g->d_table);
   ACCX_CUDA_TRY(cudaGetLastError());
   return ACCX_OK;
 }
@@ -448,12 +476,13 @@ extern "C" int accx_model_predict(accx_model *m, const float *x, uint32_t k, flo
   return ACCX_OK;
 }
 
-extern "C" int accx_bucket_stats(accx_graph *g, uint64_t *edges, double *sum_owner, double *sum_other) {
+static int bucket_stats(accx_graph *g, int mode, uint64_t *edges, double *sum_owner, double *sum_other) {
   if (!g) return ACCX_ERR_INVALID_ARG;
-  int rc = ensure_features(g, nullptr);
+  int rc = ensure_features(g, nullptr, mode);
   if (rc) return rc;
   std::vector<unsigned long long> h(3 * NBB);
-  ACCX_CUDA_TRY(cudaMemcpy(h.data(), state_of(g)->d_stats, sizeof(unsigned long long) * 3 * NBB, cudaMemcpyDeviceToHost));
+  ACCX_CUDA_TRY(cudaMemcpy(h.data(), state_of(g)->d_stats[mode], sizeof(unsigned long long) * 3 * NBB,
+                           cudaMemcpyDeviceToHost));
   for (int b = 0; b < NBB; b++) {
     if (edges) edges[b] = h[b];
     if (sum_owner) sum_owner[b] = (double)h[NBB + b];
@@ -462,21 +491,21 @@ extern "C" int accx_bucket_stats(accx_graph *g, uint64_t *edges, double *sum_own
   return ACCX_OK;
 }
 
-extern "C" int accx_bucket_features(accx_graph *g, float *features) {
+static int bucket_features(accx_graph *g, int mode, float *features) {
   if (!g || !features) return ACCX_ERR_INVALID_ARG;
-  int rc = ensure_features(g, nullptr);
+  int rc = ensure_features(g, nullptr, mode);
   if (rc) return rc;
-  ACCX_CUDA_TRY(cudaMemcpy(features, state_of(g)->d_feat, sizeof(float) * NBB * IN, cudaMemcpyDeviceToHost));
+  ACCX_CUDA_TRY(cudaMemcpy(features, state_of(g)->d_feat[mode], sizeof(float) * NBB * IN, cudaMemcpyDeviceToHost));
   return ACCX_OK;
 }
 
-extern "C" int accx_model_table_for(accx_model *m, accx_graph *g, uint8_t *table) {
+static int model_table_for(accx_model *m, accx_graph *g, int mode, uint8_t *table) {
   if (!m || !g || !table) return ACCX_ERR_INVALID_ARG;
-  int rc = ensure_features(g, nullptr);
+  int rc = ensure_features(g, nullptr, mode);
   if (rc) return rc;
   uint8_t *dt = nullptr;
   ACCX_CUDA_TRY(cudaMalloc(&dt, NBB));
-  k_model_infer<<<8, 256>>>(m->d_w, state_of(g)->d_feat, NBB, nullptr, state_of(g)->d_stats, dt);
+  k_model_infer<<<8, 256>>>(m->d_w, state_of(g)->d_feat[mode], NBB, nullptr, state_of(g)->d_stats[mode], dt);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpy(table, dt, NBB, cudaMemcpyDeviceToHost);
   cudaFree(dt);
@@ -487,10 +516,30 @@ extern "C" int accx_model_table_for(accx_model *m, accx_graph *g, uint8_t *table
   return ACCX_OK;
 }
 
-extern "C" int accx_graph_set_model(accx_graph *g, accx_model *m) {
+static int set_model(accx_graph *g, int mode, accx_model *m) {
   if (!g) return ACCX_ERR_INVALID_ARG;
   accx_graph_model_state *st = state_of(g);
   if (!st) return ACCX_ERR_OOM;
-  st->model = m;
+  st->model[mode] = m;
   return ACCX_OK;
 }
+
+extern "C" int accx_bucket_stats(accx_graph *g, uint64_t *edges, double *sum_owner, double *sum_other) {
+  return bucket_stats(g, 0, edges, sum_owner, sum_other);
+}
+extern "C" int accx_bucket_features(accx_graph *g, float *features) { return bucket_features(g, 0, features); }
+extern "C" int accx_model_table_for(accx_model *m, accx_graph *g, uint8_t *table) {
+  return model_table_for(m, g, 0, table);
+}
+extern "C" int accx_graph_set_model(accx_graph *g, accx_model *m) { return set_model(g, 0, m); }
+
+extern "C" int accx_bucket_stats_oriented(accx_graph *g, uint64_t *edges, double *sum_owner, double *sum_other) {
+  return bucket_stats(g, 1, edges, sum_owner, sum_other);
+}
+extern "C" int accx_bucket_features_oriented(accx_graph *g, float *features) {
+  return bucket_features(g, 1, features);
+}
+extern "C" int accx_model_table_for_oriented(accx_model *m, accx_graph *g, uint8_t *table) {
+  return model_table_for(m, g, 1, table);
+}
+extern "C" int accx_graph_set_model_oriented(accx_graph *g, accx_model *m) { return set_model(g, 1, m); }

@@ -25,37 +25,39 @@ from . import accx
 NB = accx.NB
 KINDS = accx.KIND_NAMES
 MODEL_PATH = os.path.join(BUILD_DIR, "sched_model.json")
+MODEL_PATH_ORIENTED = os.path.join(BUILD_DIR, "sched_model_oriented.json")
 
 
-def _count_phase_ms(G, table, reps, stream=None):
+def _count_phase_ms(G, table, reps, stream=None, orient=False):
     best = None
     for _ in range(reps):
-        G.count(policy="table", table=table, out=None, timing=True, stream=stream)
+        G.count(policy="table", table=table, out=None, timing=True, stream=stream, orient=orient)
         ph = G.timings()
         t = ph["merge"] + ph["gallop"] + ph["bitmap"]
         best = t if best is None else min(best, t)
     return best
 
 
-def bucket_timings(G, reps=2, min_edges=1, stream=None):
+def bucket_timings(G, reps=2, min_edges=1, stream=None, orient=False):
     """Exhaustive per-bucket timing.  Returns (edges[NB*NB], ms[NB*NB, 3]) with
-    NaN for buckets without owned edges."""
-    edges, _, _ = G.bucket_stats()
+    NaN for buckets without owned edges.  orient=True times the oriented kernels
+    on the oriented (prefix-length) buckets."""
+    edges, _, _ = G.bucket_stats(orient)
     skip = np.full(NB * NB, accx.KIND_SKIP, np.uint8)
-    G.count(policy="table", table=skip, out=None, stream=stream)  # warm
-    base = _count_phase_ms(G, skip, max(reps, 3), stream)
+    G.count(policy="table", table=skip, out=None, stream=stream, orient=orient)  # warm
+    base = _count_phase_ms(G, skip, max(reps, 3), stream, orient)
     T = np.full((NB * NB, 3), np.nan)
     for b in np.nonzero(edges >= min_edges)[0]:
         for k in range(3):
             t = skip.copy()
             t[b] = k
-            T[b, k] = max(_count_phase_ms(G, t, reps, stream) - base, 1e-4)
+            T[b, k] = max(_count_phase_ms(G, t, reps, stream, orient) - base, 1e-4)
     return edges, T
 
 
-def samples(G, edges, T, min_edges=32):
+def samples(G, edges, T, min_edges=32, orient=False):
     """Training rows: (features, kind, log2 seconds per edge)."""
-    X = G.bucket_features()
+    X = G.bucket_features(orient)
     xs, ks, ys = [], [], []
     for b in np.nonzero(edges >= min_edges)[0]:
         for k in range(3):
@@ -104,15 +106,15 @@ def training_graphs():
             accx.chung_lu_params(1 << 18, 24, 2.1, 20000, seed=16), accx.chung_lu_params(1 << 17, 12, 2.5, 5000, seed=17)]
 
 
-def collect(graph_params, reps=2, relabel=True, log=None):
+def collect(graph_params, reps=2, relabel=True, log=None, orient=False):
     xs, ks, ys = [], [], []
     for p in graph_params:
         t0 = time.perf_counter()
         G = accx.Graph.generate(p)
         if relabel:
             G.relabel()
-        edges, T = bucket_timings(G, reps=reps)
-        x, k, y = samples(G, edges, T)
+        edges, T = bucket_timings(G, reps=reps, orient=orient)
+        x, k, y = samples(G, edges, T, orient=orient)
         xs.append(x)
         ks.append(k)
         ys.append(y)
@@ -122,9 +124,9 @@ def collect(graph_params, reps=2, relabel=True, log=None):
     return np.concatenate(xs), np.concatenate(ks), np.concatenate(ys)
 
 
-def train_default(seed=1, epochs=4000, lr=3e-3, log=None):
+def train_default(seed=1, epochs=4000, lr=3e-3, log=None, orient=False):
     t0 = time.perf_counter()
-    x, k, y = collect(training_graphs(), log=log)
+    x, k, y = collect(training_graphs(), log=log, orient=orient)
     tc = time.perf_counter() - t0
     model = accx.Model(seed)
     loss0, _ = model.loss_grad(x, k, y)
@@ -148,19 +150,44 @@ def load(path=MODEL_PATH):
     return m, d["info"]
 
 
-def default_model(retrain=False, log=None):
-    if not retrain and os.path.exists(MODEL_PATH):
+def default_model(retrain=False, log=None, orient=False):
+    """The cost model of the direct (orient=False) or oriented kernels: loaded
+    from the build folder, else trained on the GPU and saved there."""
+    path = MODEL_PATH_ORIENTED if orient else MODEL_PATH
+    if not retrain and os.path.exists(path):
         try:
-            return load()
+            return load(path)
         except Exception:
             pass
-    model, info = train_default(log=log)
-    save(model, info)
+    model, info = train_default(log=log, orient=orient)
+    save(model, info, path)
     return model, info
 
 
-def schedule_for(G, model=None, info=None):
+def schedule_for(G, model=None, info=None, orient=False):
     """(table[NB][NB], info) chosen by the cost model for graph G."""
     if model is None:
-        model, info = default_model()
-    return model.table_for(G), dict(info or {})
+        model, info = default_model(orient=orient)
+    return model.table_for(G, orient), dict(info or {})
+
+
+def predicted_ms(G, model, orient=False):
+    """The model's predicted counting time (ms) of its own per-bucket choice:
+    sum over populated buckets of edges x 2^(predicted log2 s/edge of the
+    chosen kind)."""
+    edges, _, _ = G.bucket_stats(orient)
+    X = G.bucket_features(orient)
+    nz = np.nonzero(edges > 0)[0]
+    if len(nz) == 0:
+        return 0.0
+    y = model.predict(X[nz])
+    tab = model.table_for(G, orient).reshape(-1)[nz]
+    return float((edges[nz].astype(np.float64) * np.exp2(y[np.arange(len(nz)), tab].astype(np.float64))).sum() * 1e3)
+
+
+def plan(G, direct_model, oriented_model):
+    """Graph-level choice between direct and oriented counting by the two
+    models' predicted times, each for its own per-bucket kinds."""
+    pd = predicted_ms(G, direct_model, False)
+    po = predicted_ms(G, oriented_model, True)
+    return {"orient": po < pd, "predicted_ms": {"direct": round(pd, 3), "oriented": round(po, 3)}}

@@ -41,7 +41,8 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--scale", type=int, default=24)
     ap.add_argument("--edge-factor", type=int, default=16)
-    ap.add_argument("--policy", default="auto", help="scheduled policy: auto (trained model) or a fixed one")
+    ap.add_argument("--policy", default="auto", help="scheduled policy: auto (trained models) or a fixed one")
+    ap.add_argument("--orient", action="store_true", help="with a fixed --policy: oriented counting")
     ap.add_argument("--query-reps", type=int, default=20)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     ap.add_argument("--no-e2e", action="store_true")
@@ -138,28 +139,33 @@ class ClockSampler:
 
 
 def pick_policy(G, args):
-    """The scheduled policy: the cost model (trained on the GPU from per-bucket
-    kernel timings of small training graphs, cached in the build folder) attached
-    to the graph, so every count runs the register-resident inference kernel and
-    classifies with its table on the device."""
+    """The scheduled plan: two cost models (direct and oriented kernels, each
+    trained on the GPU from per-bucket kernel timings of small training graphs,
+    cached in the build folder) are attached to the graph; the mode whose model
+    predicts the smaller total time is chosen, and every count then runs the
+    register-resident inference kernel and classifies with its table on the
+    device.  Returns (policy, orient, {mode: model}, info)."""
     if args.policy != "auto":
-        return args.policy, None, {}
+        return args.policy, args.orient, {}, {}
     from acctricnt_gb300 import sched
     t0 = time.perf_counter()
-    model, info = sched.default_model()
-    info = dict(info)
-    info["model_ready_s"] = round(time.perf_counter() - t0, 2)
-    G.set_model(model)
-    return "model", model, info
+    md, info_d = sched.default_model(orient=False)
+    mo, info_o = sched.default_model(orient=True)
+    G.set_model(md)
+    G.set_model(mo, orient=True)
+    pl = sched.plan(G, md, mo)
+    info = {"direct_model": dict(info_d), "oriented_model": dict(info_o), "plan": pl,
+            "model_ready_s": round(time.perf_counter() - t0, 2)}
+    return "model", bool(pl["orient"]), {False: md, True: mo}, info
 
 
-def time_counts(G, policy, table, steps, warmup, tstream, world, timing=True):
+def time_counts(G, policy, table, steps, warmup, tstream, world, timing=True, orient=False):
     """K counts back to back on `tstream` (a torch.cuda.Stream, also handed to
     the library), bracketed by CUDA events on that stream."""
     import torch
     stream = tstream.cuda_stream
     for _ in range(warmup):
-        G.count(policy=policy, table=table, out=None, stream=stream)
+        G.count(policy=policy, table=table, out=None, stream=stream, orient=orient)
     torch.cuda.synchronize()
     barrier(world)
     torch.cuda.synchronize()
@@ -168,7 +174,7 @@ def time_counts(G, policy, table, steps, warmup, tstream, world, timing=True):
     phases = {}
     ev0.record(tstream)
     for _ in range(steps):
-        G.count(policy=policy, table=table, out=None, stream=stream, timing=timing)
+        G.count(policy=policy, table=table, out=None, stream=stream, timing=timing, orient=orient)
         if timing:
             for k, v in G.timings().items():
                 phases[k] = phases.get(k, 0.0) + v
@@ -194,9 +200,10 @@ def measure_queries(G, reps):
             "eps": list(QUERY_EPS), "mu": QUERY_MU}
 
 
-def measure_e2e(G, policy, table, reps, model=None):
+def measure_e2e(G, policy, table, reps, models=None, orient=False):
     """Through the C ABI with host buffers: pinned host CSR -> accx_graph_create
-    (copy + validation) -> count -> counts copied back to pinned host memory."""
+    (copy + validation) -> relabel -> count -> counts copied back to pinned host
+    memory."""
     import torch
     from acctricnt_gb300 import accx
     off, dst = G.download()
@@ -209,9 +216,9 @@ def measure_e2e(G, policy, table, reps, model=None):
         t0 = time.perf_counter()
         H = accx.Graph.from_device(t_off.data_ptr(), t_dst.data_ptr(), G.n, G.m, validate=True)
         H.relabel()
-        if model is not None:
-            H.set_model(model)
-        H.count(policy=policy, table=table, out=t_cnt.data_ptr())
+        for mode, mdl in (models or {}).items():
+            H.set_model(mdl, orient=mode)
+        H.count(policy=policy, table=table, out=t_cnt.data_ptr(), orient=orient)
         H.free()
         dt = time.perf_counter() - t0
         if i:
@@ -219,8 +226,8 @@ def measure_e2e(G, policy, table, reps, model=None):
     t = statistics.median(times)
     return {"value": round(G.m / t / 1e9, 4), "unit": UNIT, "h2d_bytes_per_step": 4 * (G.n + 1) + 4 * G.m,
             "d2h_bytes_per_step": 4 * G.m, "ms_per_step": round(t * 1e3, 3),
-            "path": "accx_graph_create(host pinned CSR, validate) + accx_graph_relabel + accx_cn_count(model policy, "
-                    "host pinned out)"}
+            "path": "accx_graph_create(host pinned CSR, validate) + accx_graph_relabel + accx_cn_count(%s policy, "
+                    "%s, host pinned out)" % (policy, "oriented" if orient else "direct")}
 
 
 class CpuSampler:
@@ -269,8 +276,14 @@ def cpu_baseline(off, dst, budget_s, nthreads):
                       % (cs.describe(stride), r["owners"], r["owned"], 100 * r["frac"], r["dt"], r["full_s"])}
 
 
-def alg_bytes(G, dominant, stats, owner_work):
-    """Algorithmic bytes of one launch of the dominant phase."""
+def alg_bytes(G, dominant, stats, owner_work, matches=None):
+    """Algorithmic bytes of one launch of the dominant phase.  Oriented bitmap
+    kernel: the ids it probed, the owner prefixes it staged, 8 bytes per owned
+    edge (partner offset and prefix length) and a 4-byte read-modify-write of a
+    count per common id found (the credit of the partner-side entry)."""
+    if dominant == "bitmap" and matches is not None:
+        found, probed = matches
+        return 4 * probed + 4 * owner_work["bitmap"] + 8 * stats["bitmap"]["edges"] + 8 * found["bitmap"]
     if dominant == "bitmap":
         e = stats["bitmap"]["edges"]
         return 4 * stats["bitmap"]["work"] + 4 * owner_work["bitmap"] + 8 * e
@@ -294,30 +307,36 @@ def run_gb300(args):
     G.relabel(stream=sp)
     torch.cuda.synchronize()
     relabel_ms = (time.perf_counter() - t0) * 1e3
-    policy, model, sched_info = pick_policy(G, args)
+    policy, orient, models, sched_info = pick_policy(G, args)
     table = None
     # correctness guard: the scheduled and plain counts are identical
-    G.count(policy=policy, table=table, out=None, stream=sp)
-    a = G.count(policy=policy, table=table, stream=sp)
+    G.count(policy=policy, table=table, out=None, stream=sp, orient=orient)
+    a = G.count(policy=policy, table=table, stream=sp, orient=orient)
     b = G.count(policy="heuristic", stream=sp)
     bit_exact = bool(np.array_equal(a, b))
     del a, b
     with ClockSampler(local) as clk:
-        ms, phases = time_counts(G, policy, table, args.steps, args.warmup, stream, world)
+        ms, phases = time_counts(G, policy, table, args.steps, args.warmup, stream, world, orient=orient)
     ms = max_over_ranks(ms, world)
     stats = G.last_stats()
     owner_work = G.owner_work()
+    matches = G.last_matches() if orient else None
     plain_ms, plain_phases = time_counts(G, "heuristic", None, args.steps, args.warmup, stream, world)
     plain_ms = max_over_ranks(plain_ms, world)
     bm_ms, _ = time_counts(G, "bitmap", None, max(1, args.steps // 2), 1, stream, world)
-    if model is not None and args.regret and rank == 0:
+    obm_ms, _ = time_counts(G, "bitmap", None, max(1, args.steps // 2), 1, stream, world, orient=True)
+    if models and args.regret and rank == 0:
         from acctricnt_gb300 import sched
         t0 = time.perf_counter()
-        edges, T = sched.bucket_timings(G, reps=1, stream=sp)
-        e, so, sp_ = G.bucket_stats()
-        mt = model.table_for(G)
+        # the other mode under its own model, measured: checks the mode choice
+        other_ms, _ = time_counts(G, policy, None, max(1, args.steps // 2), 1, stream, world, orient=not orient)
+        edges, T = sched.bucket_timings(G, reps=1, stream=sp, orient=orient)
+        e, so, sp_ = G.bucket_stats(orient)
+        mt = models[orient].table_for(G, orient)
         r = sched.regret(mt, edges, T)
-        sched_info.update({"regret": {k: round(v, 4) for k, v in r.items()},
+        sched_info.update({"mode": "oriented" if orient else "direct",
+                           "other_mode_ms": round(other_ms, 3),
+                           "regret": {k: round(v, 4) for k, v in r.items()},
                            "heuristic_bucket_sum_ms": round(sched.table_time(sched.heuristic_table(e, so, sp_), T), 3),
                            "bitmap_bucket_sum_ms": round(sched.table_time(np.full((24, 24), 2), T), 3),
                            "exhaustive_timing_s": round(time.perf_counter() - t0, 2),
@@ -325,7 +344,7 @@ def run_gb300(args):
     total_m = sum_over_ranks(G.m, world)
     value = total_m / (ms / 1e3) / 1e9
     plain_value = total_m / (plain_ms / 1e3) / 1e9
-    G.count(policy=policy, table=table, out=None, stream=sp)
+    G.count(policy=policy, table=table, out=None, stream=sp, orient=orient)
     torch.cuda.synchronize()
     scan = measure_queries(G, args.query_reps)
     peaks = {}
@@ -336,23 +355,25 @@ def run_gb300(args):
     peak = float(peaks.get("hbm_gbs", 6800.0))
     dominant = max(("merge", "gallop", "bitmap", "mirror", "plan"), key=lambda k: phases.get(k, 0.0))
     dom_ms = phases.get(dominant, 0.0)
-    ab = alg_bytes(G, dominant, stats, owner_work)
+    ab = alg_bytes(G, dominant, stats, owner_work, matches if dominant == "bitmap" else None)
     achieved = ab / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else None
+    kname = dominant + ("_or" if orient and dominant in ("merge", "gallop", "bitmap") else "")
     traffic = None
     try:
-        tr = json.load(open(os.path.join(ROOT, "profiles", "traffic.json"))).get(dominant)
+        tr = json.load(open(os.path.join(ROOT, "profiles", "traffic.json"))).get(kname)
         if tr:  # bytes per probed id measured by ncu on a smaller case, times this launch's probes
-            traffic = int(tr["bytes_per_probe"] * stats[dominant]["work"])
+            probes = matches[1] if (orient and dominant == "bitmap") else stats[dominant]["work"]
+            traffic = int(tr["bytes_per_probe"] * probes)
     except Exception:
         pass
-    roofline = {"bound": "hbm", "kernel": "k_" + dominant, "achieved": round(achieved, 1) if achieved else None,
+    roofline = {"bound": "hbm", "kernel": "k_" + kname, "achieved": round(achieved, 1) if achieved else None,
                 "peak": peak, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback",
                 "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None, "traffic": traffic,
                 "alg_bytes_per_launch": int(ab), "launch_ms": round(dom_ms, 3),
                 "merge_equiv_bytes": int(4 * float(np.sum(np.diff(G.download()[0]).astype(np.float64) ** 2)) + 4 * G.m)}
     e2e = None
     if not args.no_e2e and rank == 0:
-        e2e = measure_e2e(G, policy, table, 2, model)
+        e2e = measure_e2e(G, policy, table, 2, models, orient)
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
         off, dst = G.download()
@@ -362,17 +383,20 @@ def run_gb300(args):
             "vs_baseline": None, "dtype": "int32", "data": "synthetic",
             "config": {"workload": "R-MAT scale %d, edge factor %d, (0.57,0.19,0.19,0.05), seed 1+rank; all-edge CN "
                                    "count; SCAN eps %s mu %d" % (args.scale, args.edge_factor, list(QUERY_EPS), QUERY_MU),
-                       "n": G.n, "m": G.m, "policy": policy, "parallelism": "replicas%d" % world,
+                       "n": G.n, "m": G.m, "policy": policy, "orient": orient, "parallelism": "replicas%d" % world,
                        "l2": "inputs larger than L2 (CSR %.2f GB, counts %.2f GB)" % ((4 * G.m + 4 * G.n) / 1e9,
                                                                                    4 * G.m / 1e9)},
             "plain": {"policy": "heuristic", "value": round(plain_value, 4), "ms_per_step": round(plain_ms, 3),
                       "phases_ms": {k: round(v, 3) for k, v in plain_phases.items()}},
             "speedup_vs_plain": round(plain_ms / ms, 3), "bit_exact_vs_plain": bit_exact,
             "bitmap_all": {"ms_per_step": round(bm_ms, 3), "value": round(total_m / (bm_ms / 1e3) / 1e9, 4)},
+            "oriented_bitmap_all": {"ms_per_step": round(obm_ms, 3), "value": round(total_m / (obm_ms / 1e3) / 1e9, 4)},
             "relabel_ms": round(relabel_ms, 2),
             "phases_ms": {k: round(v, 3) for k, v in phases.items()}, "kinds": stats,
+            "matches": ({"found": matches[0], "bitmap_probed": matches[1]} if matches else None),
             "scan": scan, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-            "gpu_launches": (8 if policy == "model" else 7) * args.steps, "clocks": clk.summary(),
+            "gpu_launches": ((8 if policy == "model" else 7) + (1 if orient else 0)) * args.steps,
+            "clocks": clk.summary(),
             "sched": sched_info}
     if rank == 0:
         print(json.dumps(line), flush=True)

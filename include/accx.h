@@ -172,6 +172,15 @@ typedef struct {
   int sparse_table_kb;    /* hashed bitmap-word table for the other ids, KiB (0 = tuned default) */
   int sm_limit;           /* run the persistent counting kernels on at most this many SMs (0 = all);
                              leaves SMs free for latency-critical work on other streams */
+  int orient;             /* 0: direct -- every owned edge intersects the two full lists.
+                             1: oriented -- |N(u) ∩ N(v)| is the number of triangles on (u,v); each
+                             triangle a<b<c is found once, from the edge (c,b), by intersecting the
+                             prefix lists N(c) ∩ [0,b) and N(b) ∩ [0,b), and credited to its three
+                             edges.  Edge owners, buckets and kinds then use prefix lengths (neighbours
+                             with smaller ids) instead of degrees.  Exact either way; oriented does far
+                             less work on a degree-descending relabeled graph (accx_graph_relabel),
+                             where prefix lists hold at most sqrt(2m) ids.  ACCX_POLICY_MODEL then uses
+                             the model attached by accx_graph_set_model_oriented. */
 } accx_count_opts;
 
 /* Counts cnt[e] = |N(u) ∩ N(v)| + bias for every CSR entry e=(u,v) into the
@@ -194,6 +203,11 @@ int accx_cn_last_stats(const accx_graph *g, uint64_t edges[ACCX_NUM_KINDS], uint
 /* Owner-side elements per kind of the last count: sum of owner degrees over the
  * merge/gallop edges, and the owner lists the bitmap kernel staged (per work item). */
 int accx_cn_last_owner_work(const accx_graph *g, uint64_t owner_work[ACCX_NUM_KINDS]);
+
+/* Oriented counts: common ids found per kind (each a triangle) in the last
+ * count, and the ids the bitmap kind actually probed (partner prefixes after the
+ * cut at the smaller id).  Zero after a direct count. */
+int accx_cn_last_matches(const accx_graph *g, uint64_t matches[ACCX_NUM_KINDS], uint64_t *probed);
 
 /* Phases timed when accx_count_opts.timing is set. */
 #define ACCX_PHASE_PLAN 0    /* classify + bitmap work items */
@@ -261,6 +275,14 @@ int accx_model_predict(accx_model *m, const float *x, uint32_t k, float *y);
 int accx_model_table_for(accx_model *m, accx_graph *g, uint8_t *table);
 /* Attach a model to a graph handle for ACCX_POLICY_MODEL (the handle does not own it). */
 int accx_graph_set_model(accx_graph *g, accx_model *m);
+/* The same for oriented counts (accx_count_opts.orient = 1): buckets by prefix
+ * length (owner = longer prefix; edges whose shorter prefix is empty left out) on
+ * the CSR counts run on -- the relabeled copy when there is one.  The oriented
+ * kernels have their own costs, so they get their own model. */
+int accx_bucket_stats_oriented(accx_graph *g, uint64_t *edges, double *sum_owner, double *sum_other);
+int accx_bucket_features_oriented(accx_graph *g, float *features);
+int accx_model_table_for_oriented(accx_model *m, accx_graph *g, uint8_t *table);
+int accx_graph_set_model_oriented(accx_graph *g, accx_model *m);
 
 /* ---- batches of uneven graphs -------------------------------------------------
  * No reference counterpart (the reference counts one graph per process).  A

@@ -132,6 +132,8 @@ def _load():
         "accx_model_table_for": (C.c_int, [P, P, P]),
         "accx_graph_set_model": (C.c_int, [P, P]),
         "accx_cn_last_matches": (C.c_int, [P, P, P]),
+        "accx_model_set_kind_bias": (C.c_int, [P, P]),
+        "accx_model_get_kind_bias": (C.c_int, [P, P]),
         "accx_bucket_stats_oriented": (C.c_int, [P, P, P, P]),
         "accx_bucket_features_oriented": (C.c_int, [P, P]),
         "accx_model_table_for_oriented": (C.c_int, [P, P, P]),
@@ -522,6 +524,15 @@ class Model:
         _check(lib.accx_model_train(self._h, _ptr(x), _ptr(kind), _ptr(target), len(kind), int(epochs), float(lr),
                                     C.byref(loss)), "model_train")
         return float(loss.value)
+
+    def kind_bias(self):
+        b = np.zeros(MODEL_OUT, np.float32)
+        _check(lib.accx_model_get_kind_bias(self._h, _ptr(b)), "model_get_kind_bias")
+        return b
+
+    def set_kind_bias(self, bias):
+        b = np.ascontiguousarray(bias, np.float32).reshape(MODEL_OUT)
+        _check(lib.accx_model_set_kind_bias(self._h, _ptr(b)), "model_set_kind_bias")
 
     def predict(self, x):
         x = np.ascontiguousarray(x, np.float32).reshape(-1, MODEL_IN)

@@ -44,6 +44,11 @@ struct accx_model {
   float *d_grad = nullptr;    // NP
   float *d_loss = nullptr;    // 1
   int step = 0;
+  float bias[OUT] = {0.f, 0.f, 0.f};  // per-kind log2 offsets added before the argmin of a table
+};
+
+struct accx_kind_bias {
+  float b[OUT];
 };
 
 // ---------------------------------------------------------------------------
@@ -144,7 +149,7 @@ __global__ void k_model_adam(float *__restrict__ master, __half *__restrict__ w,
 __global__ void __launch_bounds__(256) k_model_infer(const __half *__restrict__ w, const float *__restrict__ x,
                                                      uint32_t k, float *__restrict__ y,
                                                      const unsigned long long *__restrict__ edges,
-                                                     uint8_t *__restrict__ table) {
+                                                     uint8_t *__restrict__ table, accx_kind_bias kb) {
   const int lane = threadIdx.x & 31;
   float w1[IN], w2[H], w3[OUT], b3[OUT];
 #pragma unroll
@@ -181,7 +186,7 @@ __global__ void __launch_bounds__(256) k_model_infer(const __half *__restrict__ 
         int best = 0;
 #pragma unroll
         for (int o = 1; o < OUT; o++)
-          if (out[o] < out[best]) best = o;
+          if (out[o] + kb.b[o] < out[best] + kb.b[best]) best = o;
         table[r] = (edges && edges[r] == 0) ? (uint8_t)ACCX_KIND_MERGE : (uint8_t)best;
       } else {
 #pragma unroll
@@ -313,7 +318,10 @@ int accx_model_table_device(accx_graph *g, cudaStream_t s, int orient) {
   if (!st || !st->model[mode]) return ACCX_ERR_NOT_READY;
   int rc = ensure_features(g, s, mode);
   if (rc) return rc;
-  k_model_infer<<<8, 256, 0, s>>>(st->model[mode]->d_w, st->d_feat[mode], NBB, nullptr, st->d_stats[mode], g->d_table);
+  accx_kind_bias kb;
+  for (int o = 0; o < OUT; o++) kb.b[o] = st->model[mode]->bias[o];
+  k_model_infer<<<8, 256, 0, s>>>(st->model[mode]->d_w, st->d_feat[mode], NBB, nullptr, st->d_stats[mode], g->d_table,
+                                  kb);
   ACCX_CUDA_TRY(cudaGetLastError());
   return ACCX_OK;
 }
@@ -463,7 +471,7 @@ extern "C" int accx_model_predict(accx_model *m, const float *x, uint32_t k, flo
   cudaError_t e = cudaMalloc(&dy, sizeof(float) * (size_t)k * OUT);
   if (e == cudaSuccess) e = cudaMemcpy(dx, x, sizeof(float) * (size_t)k * IN, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) {
-    k_model_infer<<<8, 256>>>(m->d_w, dx, k, dy, nullptr, nullptr);
+    k_model_infer<<<8, 256>>>(m->d_w, dx, k, dy, nullptr, nullptr, accx_kind_bias{});
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaMemcpy(y, dy, sizeof(float) * (size_t)k * OUT, cudaMemcpyDeviceToHost);
@@ -505,7 +513,9 @@ static int model_table_for(accx_model *m, accx_graph *g, int mode, uint8_t *tabl
   if (rc) return rc;
   uint8_t *dt = nullptr;
   ACCX_CUDA_TRY(cudaMalloc(&dt, NBB));
-  k_model_infer<<<8, 256>>>(m->d_w, state_of(g)->d_feat[mode], NBB, nullptr, state_of(g)->d_stats[mode], dt);
+  accx_kind_bias kb;
+  for (int o = 0; o < OUT; o++) kb.b[o] = m->bias[o];
+  k_model_infer<<<8, 256>>>(m->d_w, state_of(g)->d_feat[mode], NBB, nullptr, state_of(g)->d_stats[mode], dt, kb);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpy(table, dt, NBB, cudaMemcpyDeviceToHost);
   cudaFree(dt);
@@ -526,6 +536,21 @@ static int set_model(accx_graph *g, int mode, accx_model *m) {
 
 extern "C" int accx_bucket_stats(accx_graph *g, uint64_t *edges, double *sum_owner, double *sum_other) {
   return bucket_stats(g, 0, edges, sum_owner, sum_other);
+}
+
+extern "C" int accx_model_set_kind_bias(accx_model *m, const float *bias) {
+  if (!m || !bias) return ACCX_ERR_INVALID_ARG;
+  for (int o = 0; o < OUT; o++) {
+    if (!(bias[o] > -1e6f && bias[o] < 1e6f)) return ACCX_ERR_INVALID_ARG;
+    m->bias[o] = bias[o];
+  }
+  return ACCX_OK;
+}
+
+extern "C" int accx_model_get_kind_bias(const accx_model *m, float *bias) {
+  if (!m || !bias) return ACCX_ERR_INVALID_ARG;
+  for (int o = 0; o < OUT; o++) bias[o] = m->bias[o];
+  return ACCX_OK;
 }
 extern "C" int accx_bucket_features(accx_graph *g, float *features) { return bucket_features(g, 0, features); }
 extern "C" int accx_model_table_for(accx_model *m, accx_graph *g, uint8_t *table) {

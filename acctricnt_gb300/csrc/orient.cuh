@@ -19,6 +19,8 @@
 // Included by count.cu after the shared counting definitions.
 #pragma once
 
+#define LONG_UNROLL 8  // loads in flight per lane on long probe lists
+
 // pre[u] = |N(u) ∩ [0, u)|.
 __global__ void k_pre(const uint32_t *__restrict__ off, const int32_t *__restrict__ dst, uint32_t n,
                       uint32_t *__restrict__ pre) {
@@ -283,28 +285,29 @@ __global__ void __launch_bounds__(1024, 1) k_bitmap_or(const uint32_t *__restric
         q = __shfl_sync(ACCX_FULL_MASK, q, 0);
         if (q >= nlong) break;
         const uint32_t a0 = s_lbeg[q], a1 = a0 + s_llen[q];
-        const uint32_t al = min(a1, (a0 + 3u) & ~3u), bl4 = max(al, a1 & ~3u);
         uint32_t h = 0;
-        auto probe = [&](int32_t v, uint32_t j) {
-          const uint32_t id = (uint32_t)v;
-          if (v >= 0 && id < W) {
-            const uint32_t wd = words[id >> 5], bit = 1u << (id & 31);
-            if (wd & bit) {
-              const uint32_t rk = wbase[id >> 5] + __popc(wd & (bit - 1u));
-              h++;
-              atomicAdd(cnt + j, 1);
-              if (rk < pxs) atomicAdd(&ocnt[rk], 1u);
+        // lane-consecutive ids, LONG_UNROLL loads in flight per lane: a warp's
+        // credits for one load land in one 128-byte line of cnt
+        for (uint32_t j0 = a0; j0 < a1; j0 += 32u * LONG_UNROLL) {
+          int32_t v[LONG_UNROLL];
+#pragma unroll
+          for (int r = 0; r < LONG_UNROLL; r++) {
+            const uint32_t j = j0 + 32u * r + (uint32_t)lane;
+            v[r] = j < a1 ? __ldg(dst + j) : -1;
+          }
+#pragma unroll
+          for (int r = 0; r < LONG_UNROLL; r++) {
+            const uint32_t id = (uint32_t)v[r];
+            if (v[r] >= 0 && id < W) {
+              const uint32_t wd = words[id >> 5], bit = 1u << (id & 31);
+              if (wd & bit) {
+                const uint32_t rk = wbase[id >> 5] + __popc(wd & (bit - 1u));
+                h++;
+                atomicAdd(cnt + j0 + 32u * r + (uint32_t)lane, 1);
+                if (rk < pxs) atomicAdd(&ocnt[rk], 1u);
+              }
             }
           }
-        };
-        if (a0 + (uint32_t)lane < al) probe(__ldg(dst + a0 + lane), a0 + lane);
-        if (bl4 + (uint32_t)lane < a1) probe(__ldg(dst + bl4 + lane), bl4 + lane);
-        for (uint32_t jj = al + 4u * (uint32_t)lane; jj < bl4; jj += 128u) {
-          const int4 q0 = __ldg(reinterpret_cast<const int4 *>(dst + jj));
-          probe(q0.x, jj);
-          probe(q0.y, jj + 1);
-          probe(q0.z, jj + 2);
-          probe(q0.w, jj + 3);
         }
         h = __reduce_add_sync(ACCX_FULL_MASK, h);
         if (lane == 0) found += h;

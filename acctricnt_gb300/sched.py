@@ -38,18 +38,33 @@ def _count_phase_ms(G, table, reps, stream=None, orient=False):
     return best
 
 
-def bucket_timings(G, reps=2, min_edges=1, stream=None, orient=False):
-    """Exhaustive per-bucket timing.  Returns (edges[NB*NB], ms[NB*NB, 3]) with
-    NaN for buckets without owned edges.  orient=True times the oriented kernels
-    on the oriented (prefix-length) buckets."""
+def bucket_timings(G, reps=2, min_edges=1, stream=None, orient=False, context=None):
+    """Per-bucket timing.  Returns (edges[NB*NB], ms[NB*NB, 3]) with NaN for
+    buckets not timed (fewer than min_edges owned edges).  orient=True times the
+    oriented kernels on the oriented (prefix-length) buckets.
+
+    context=None: every other bucket skipped (the bucket alone; low noise, but it
+    overstates the bitmap kind, whose kernel stages an owner once for all of the
+    owner's buckets -- calibrate() corrects that with a kind bias fitted on whole
+    counts).  context="bitmap": the marginal cost of bucket b under kind k while
+    every other populated bucket runs the bitmap kind, time(b -> k) - time(b
+    skipped); on large graphs most buckets' marginal costs are below the noise of
+    one whole count."""
     edges, _, _ = G.bucket_stats(orient)
     skip = np.full(NB * NB, accx.KIND_SKIP, np.uint8)
-    G.count(policy="table", table=skip, out=None, stream=stream, orient=orient)  # warm
-    base = _count_phase_ms(G, skip, max(reps, 3), stream, orient)
+    base_table = skip.copy()
+    if context == "bitmap":
+        base_table[edges > 0] = accx.KIND_BITMAP
+    G.count(policy="table", table=base_table, out=None, stream=stream, orient=orient)  # warm
+    base_all = None
+    if context is None:
+        base_all = _count_phase_ms(G, skip, max(reps, 3), stream, orient)
     T = np.full((NB * NB, 3), np.nan)
-    for b in np.nonzero(edges >= min_edges)[0]:
+    for b in np.nonzero(edges >= max(min_edges, 1))[0]:
+        t = base_table.copy()
+        t[b] = accx.KIND_SKIP
+        base = base_all if base_all is not None else _count_phase_ms(G, t, reps, stream, orient)
         for k in range(3):
-            t = skip.copy()
             t[b] = k
             T[b, k] = max(_count_phase_ms(G, t, reps, stream, orient) - base, 1e-4)
     return edges, T
@@ -124,7 +139,37 @@ def collect(graph_params, reps=2, relabel=True, log=None, orient=False):
     return np.concatenate(xs), np.concatenate(ks), np.concatenate(ys)
 
 
-def train_default(seed=1, epochs=4000, lr=3e-3, log=None, orient=False):
+def calibration_graphs():
+    return training_graphs() + [accx.rmat_params(20, 16, seed=18)]
+
+
+BITMAP_OFFSETS = (0.0, -0.5, -1.0, -1.5, -2.0, -3.0, -5.0, -64.0)
+
+
+def calibrate(model, graph_params, orient=False, reps=3, offsets=BITMAP_OFFSETS, log=None):
+    """Fits the bitmap kind's log2 offset on whole counts: for every candidate
+    offset the model's table is run as a whole count on every calibration graph
+    (relabeled), and the offset with the smallest sum of times relative to each
+    graph's best candidate is kept (ties: the smaller offset).  -64 amounts to
+    the bitmap kind for every bucket."""
+    rel = np.zeros((len(graph_params), len(offsets)))
+    for gi, p in enumerate(graph_params):
+        G = accx.Graph.generate(p)
+        G.relabel()
+        for ci, off in enumerate(offsets):
+            model.set_kind_bias([0.0, 0.0, off])
+            rel[gi, ci] = _count_phase_ms(G, model.table_for(G, orient).reshape(-1), reps, None, orient)
+        G.free()
+    score = (rel / rel.min(1, keepdims=True)).sum(0)
+    best = int(np.argmin(score))
+    model.set_kind_bias([0.0, 0.0, offsets[best]])
+    if log:
+        log("calibrated bitmap offset %.2f (scores %s)" % (offsets[best], np.round(score, 3).tolist()))
+    return {"kind_bias": [0.0, 0.0, float(offsets[best])], "offsets": list(offsets),
+            "relative_time": [round(float(v) / len(graph_params), 4) for v in score]}
+
+
+def train_default(seed=1, epochs=4000, lr=3e-3, log=None, orient=False, calibrate_bias=True):
     t0 = time.perf_counter()
     x, k, y = collect(training_graphs(), log=log, orient=orient)
     tc = time.perf_counter() - t0
@@ -134,12 +179,16 @@ def train_default(seed=1, epochs=4000, lr=3e-3, log=None, orient=False):
     loss = model.train(x, k, y, epochs=epochs, lr=lr)
     info = {"rows": int(len(k)), "collect_s": round(tc, 2), "train_s": round(time.perf_counter() - t1, 2),
             "epochs": epochs, "loss_initial": loss0, "loss_final": loss}
+    if calibrate_bias:
+        t2 = time.perf_counter()
+        info["calibration"] = calibrate(model, calibration_graphs(), orient=orient, log=log)
+        info["calibration"]["seconds"] = round(time.perf_counter() - t2, 2)
     return model, info
 
 
 def save(model, info, path=MODEL_PATH):
     with open(path, "w") as f:
-        json.dump({"params": model.params().tolist(), "info": info}, f)
+        json.dump({"params": model.params().tolist(), "kind_bias": model.kind_bias().tolist(), "info": info}, f)
 
 
 def load(path=MODEL_PATH):
@@ -147,6 +196,7 @@ def load(path=MODEL_PATH):
         d = json.load(f)
     m = accx.Model(1)
     m.set_params(np.array(d["params"], np.float32))
+    m.set_kind_bias(np.array(d.get("kind_bias", [0, 0, 0]), np.float32))
     return m, d["info"]
 
 

@@ -276,6 +276,15 @@ def cpu_baseline(off, dst, budget_s, nthreads):
                       % (cs.describe(stride), r["owners"], r["owned"], 100 * r["frac"], r["dt"], r["full_s"])}
 
 
+def measured_regret(model_ms, alternatives):
+    """The scheduled count against the fastest whole count measured among the
+    alternatives: (model - best) / best, 0 when the model is the fastest."""
+    name, best = min(alternatives.items(), key=lambda kv: kv[1])
+    b = min(best, model_ms)
+    return {"best": name if best < model_ms else "model", "best_ms": round(b, 3),
+            "frac": round((model_ms - b) / b, 4) if b > 0 else 0.0}
+
+
 def alg_bytes(G, dominant, stats, owner_work, matches=None):
     """Algorithmic bytes of one launch of the dominant phase.  Oriented bitmap
     kernel: the ids it probed, the owner prefixes it staged, 8 bytes per owned
@@ -334,8 +343,16 @@ def run_gb300(args):
         e, so, sp_ = G.bucket_stats(orient)
         mt = models[orient].table_for(G, orient)
         r = sched.regret(mt, edges, T)
+        # the per-bucket best table, run as a whole count (the additive estimate checked)
+        best_tab = sched.exhaustive_table(edges, T).reshape(-1).copy()
+        best_tab[~np.isfinite(T).all(1)] = mt.reshape(-1)[~np.isfinite(T).all(1)]
+        best_ms, _ = time_counts(G, "table", best_tab, max(1, args.steps // 2), 1, stream, world, orient=orient)
         sched_info.update({"mode": "oriented" if orient else "direct",
                            "other_mode_ms": round(other_ms, 3),
+                           "best_table_count_ms": round(best_ms, 3),
+                           "measured_regret": measured_regret(ms, {"per_bucket_best_table": best_ms,
+                                                                   "oriented_bitmap_all": obm_ms,
+                                                                   "direct_bitmap_all": bm_ms}),
                            "regret": {k: round(v, 4) for k, v in r.items()},
                            "heuristic_bucket_sum_ms": round(sched.table_time(sched.heuristic_table(e, so, sp_), T), 3),
                            "bitmap_bucket_sum_ms": round(sched.table_time(np.full((24, 24), 2), T), 3),

@@ -271,8 +271,15 @@ int accx_model_train(accx_model *m, const float *x, const int32_t *kind, const f
                      int epochs, float lr, float *final_loss);
 /* Predictions (log2 seconds per edge, ACCX_MODEL_OUT per row) for k feature rows. */
 int accx_model_predict(accx_model *m, const float *x, uint32_t k, float *y);
-/* The kind table the model picks for a graph (runs on the device). */
+/* The kind table the model picks for a graph (runs on the device): per bucket
+ * the kind with the smallest prediction + kind bias. */
 int accx_model_table_for(accx_model *m, accx_graph *g, uint8_t *table);
+/* Per-kind log2 offsets added to the predictions before a table's argmin
+ * (default 0).  Per-bucket timings taken with the other buckets skipped
+ * overstate the bitmap kind, whose owner staging serves all of an owner's
+ * buckets; the scheduler fits this offset on whole-count timings. */
+int accx_model_set_kind_bias(accx_model *m, const float *bias);
+int accx_model_get_kind_bias(const accx_model *m, float *bias);
 /* Attach a model to a graph handle for ACCX_POLICY_MODEL (the handle does not own it). */
 int accx_graph_set_model(accx_graph *g, accx_model *m);
 /* The same for oriented counts (accx_count_opts.orient = 1): buckets by prefix

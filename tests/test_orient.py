@@ -143,3 +143,22 @@ def test_learned_oriented_schedule_on_an_unseen_graph():
     direct, _ = sched.train_default(epochs=500)
     pl = sched.plan(G, direct, model)
     assert set(pl["predicted_ms"]) == {"direct", "oriented"} and pl["predicted_ms"]["oriented"] > 0
+
+
+def test_kind_bias_steers_the_table():
+    m = accx.Model(seed=8)
+    G = accx.Graph.generate(accx.rmat_params(14, 16, seed=5))
+    ref = G.count(policy="heuristic")
+    G.relabel()
+    e, _, _ = G.bucket_stats(orient=True)
+    m.set_kind_bias([0.0, 0.0, -64.0])
+    assert np.allclose(m.kind_bias(), [0, 0, -64])
+    t = m.table_for(G, orient=True).reshape(-1)
+    assert (t[e > 0] == accx.KIND_BITMAP).all()
+    m.set_kind_bias([0.0, -64.0, 0.0])
+    t = m.table_for(G, orient=True).reshape(-1)
+    assert (t[e > 0] == accx.KIND_GALLOP).all()
+    G.set_model(m, orient=True)
+    assert np.array_equal(G.count(policy="model", orient=True), ref)
+    with pytest.raises(accx.AccxError):
+        m.set_kind_bias([0.0, float("nan"), 0.0])

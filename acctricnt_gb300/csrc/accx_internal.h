@@ -70,6 +70,10 @@ struct accx_graph {
   unsigned long long *d_icnt = nullptr;    // n+1 bitmap items per owner
   unsigned long long *d_prefix = nullptr;  // n+1 exclusive prefix of d_icnt
   uint32_t *d_pre = nullptr;               // n prefix lengths (neighbours with smaller ids), oriented counts
+  uint2 *d_or_sl = nullptr;                // m oriented bitmap entries: (partner prefix start, cut length), 0 length = not bitmap
+  uint32_t *d_or_items = nullptr;          // n + m/32 + 1 oriented bitmap work items: owner of each
+  uint32_t *d_rev = nullptr;               // m reverse entry of every entry of the counting CSR (oriented counts)
+  const uint32_t *rev_csr = nullptr;       // the offsets array d_rev was built for
   void *d_scan_tmp = nullptr;
   size_t scan_tmp_bytes = 0;
   unsigned long long *d_counters = nullptr;  // [0] merge, [1] gallop, [2] bitmap items, [3..5] work per kind

@@ -67,7 +67,8 @@ __global__ void __launch_bounds__(TILE) k_classify(const uint32_t *__restrict__ 
                                                    const uint8_t *__restrict__ table, uint2 *__restrict__ list,
                                                    uint32_t list_cap, unsigned long long *__restrict__ work_u,
                                                    unsigned long long *__restrict__ ctr, const uint32_t *__restrict__ pre,
-                                                   uint32_t bm_idlim, uint32_t bm_pcap) {
+                                                   uint32_t bm_idlim, uint32_t bm_pcap, uint2 *__restrict__ or_sl,
+                                                   const uint32_t *__restrict__ rev) {
   __shared__ accx_tile_rows<TILE> sh;
   __shared__ uint8_t s_table[ACCX_NB * ACCX_NB];
   if (policy == ACCX_POLICY_TABLE || policy == ACCX_POLICY_MODEL)
@@ -91,6 +92,23 @@ __global__ void __launch_bounds__(TILE) k_classify(const uint32_t *__restrict__ 
       dv = off[v + 1] - off[v];
       if (accx_owns(u, du, v, dv)) kind = accx_edge_kind(policy, s_table, du, dv);
     }
+  }
+  // oriented bitmap entries: the partner's prefix start and its length cut at
+  // min(u, v), stored for the bitmap kernel's rounds
+  uint32_t bwork = dv;
+  if (ORIENT && e < m) {
+    uint2 sl = make_uint2(0u, 0u);
+    if (kind == ACCX_KIND_BITMAP) {
+      const uint32_t sst = off[v];
+      uint32_t t = sst + dv;
+      if (v > u) {  // cut P(v) at u: u's position in N(v) is the reverse entry
+        const uint32_t r = rev[e];
+        t = (r >= sst && r < t) ? r : sst;
+      }
+      sl = make_uint2(sst, t - sst);
+      bwork = t - sst;
+    }
+    or_sl[e] = sl;
   }
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
@@ -125,7 +143,7 @@ __global__ void __launch_bounds__(TILE) k_classify(const uint32_t *__restrict__ 
     if (k == ACCX_KIND_BITMAP && kind == k) {
       // aggregate the owner's probe work per row before the atomic
       unsigned peers = __match_any_sync(mask, u);
-      unsigned sw = __reduce_add_sync(peers, dv);
+      unsigned sw = __reduce_add_sync(peers, bwork);
       if (lane == __ffs(peers) - 1) atomicAdd(&work_u[u], (unsigned long long)sw + 1ull);
     }
   }
@@ -595,7 +613,7 @@ int accx_prefix_lengths(accx_graph *g, cudaStream_t s) {
 static int g_block_warps = 32;
 static int g_dense_kb = 128;
 static int g_sparse_kb = 64;
-static int g_or_dense_kb = 96;
+static int g_or_dense_kb = 64;
 static int g_or_counter_kb = 16;
 
 
@@ -659,28 +677,49 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s)
     const uint32_t pcap = (uint32_t)skb * 256u;     // owner-prefix counters
     const size_t smem = (size_t)W / 8u + (size_t)pcap * 4u + (size_t)W / 16u;
     const uint32_t target = ITEM_TARGET_DEFAULT;
+    // per-entry bitmap work and the item array (n + m/32 + 1 bounds the items:
+    // an owner is cut into at most max(1, degree/32) slices)
+    const uint32_t items_cap = n + m / 32u + 1u;
+    if (!g->d_or_sl || !g->d_or_items || !g->d_rev) {
+      if (!g->d_or_sl) ACCX_CUDA_TRY(accx_dev_alloc((void **)&g->d_or_sl, sizeof(uint2) * (size_t)m, g->home));
+      if (!g->d_or_items)
+        ACCX_CUDA_TRY(accx_dev_alloc((void **)&g->d_or_items, sizeof(uint32_t) * (size_t)items_cap, g->home));
+      if (!g->d_rev) ACCX_CUDA_TRY(accx_dev_alloc((void **)&g->d_rev, sizeof(uint32_t) * (size_t)m, g->home));
+      g->rev_csr = nullptr;
+      if (g->home) ACCX_CUDA_TRY(cudaStreamSynchronize(g->home));
+    }
     k_pre<<<sms * 8, 256, 0, s>>>(off, dst, n, g->d_pre);
+    // reverse entries: built on the first oriented count of this CSR and kept
+    // (an index of the graph, like the tile rows)
+    if (g->rev_csr != off) {
+      ACCX_CUDA_TRY(cudaMemsetAsync(g->d_rev, 0xff, sizeof(uint32_t) * (size_t)m, s));
+      k_rev_build<256><<<tiles, 256, 0, s>>>(off, tilerow, dst, g->d_pre, n, m, g->d_rev);
+      g->rev_csr = off;
+    }
     k_classify<256, true><<<tiles, 256, 0, s>>>(off, tilerow, dst, n, m, policy, g->d_table, g->d_edge_list, list_cap,
-                                                work_u, ctr, g->d_pre, W, pcap);
+                                                work_u, ctr, g->d_pre, W, pcap, g->d_or_sl, g->d_rev);
     k_item_counts<<<sms * 4, 256, 0, s>>>(off, dst, n, work_u, W, 1, target, g->d_icnt, ctr, g->d_pre);
     ACCX_CUDA_TRY(cub::DeviceScan::ExclusiveSum(g->d_scan_tmp, g->scan_tmp_bytes, g->d_icnt, g->d_prefix,
                                                 (int64_t)n + 1, s));
+    k_item_fill<<<sms * 4, 256, 0, s>>>(g->d_icnt, g->d_prefix, n, items_cap, g->d_or_items);
     ACCX_MARK(1);
-    k_merge_or<<<sms * 8, MERGE_WARPS * 32, 0, s>>>(off, dst, g->d_pre, g->d_edge_list, list_cap, ctr, cnt);
+    k_merge_or<<<sms * 8, MERGE_WARPS * 32, 0, s>>>(off, dst, g->d_pre, g->d_rev, g->d_edge_list, list_cap, ctr,
+                                                    cnt);
     ACCX_MARK(2);
-    k_gallop_or<<<sms * 8, MERGE_WARPS * 32, 0, s>>>(off, dst, g->d_pre, g->d_edge_list, list_cap, ctr, cnt);
+    k_gallop_or<<<sms * 8, MERGE_WARPS * 32, 0, s>>>(off, dst, g->d_pre, g->d_rev, g->d_edge_list, list_cap, ctr,
+                                                     cnt);
     ACCX_MARK(3);
     ACCX_CUDA_TRY(cudaFuncSetAttribute(k_bitmap_or, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     ACCX_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bitmap_or, warps * 32, smem));
     if (per_sm < 1) return ACCX_ERR_INVALID_ARG;
-    k_bitmap_or<<<sms * per_sm, warps * 32, smem, s>>>(off, dst, g->d_pre, n, policy, g->d_table, work_u, g->d_prefix,
-                                                       W, pcap, target, cnt, ctr);
+    k_bitmap_or<<<sms * per_sm, warps * 32, smem, s>>>(off, dst, g->d_pre, n, g->d_or_items, items_cap, work_u,
+                                                       g->d_prefix, g->d_or_sl, W, pcap, target, cnt, ctr);
     ACCX_MARK(4);
-    k_combine_or<256><<<tiles, 256, 0, s>>>(off, tilerow, dst, g->d_pre, n, m, bias, cnt);
+    k_combine_or<<<sms * 8, 256, 0, s>>>(m, g->d_rev, bias, cnt);
   } else {
     k_classify<256, false><<<tiles, 256, 0, s>>>(off, tilerow, dst, n, m, policy, g->d_table, g->d_edge_list, list_cap,
-                                                 work_u, ctr, nullptr, 0u, 0u);
+                                                 work_u, ctr, nullptr, 0u, 0u, nullptr, nullptr);
     const uint32_t W = (uint32_t)dkb * 8192u;        // dense ids (bits)
     const uint32_t S = (uint32_t)skb * 1024u / 8u;   // sparse 8-byte slots
     const size_t smem = (size_t)W / 8u + (size_t)S * 8u;

@@ -30,22 +30,54 @@ __global__ void k_pre(const uint32_t *__restrict__ off, const int32_t *__restric
   }
 }
 
+// Reverse entries: rev[e] = position of u in N(v) for every entry e = (u,v).
+// One thread per entry e = (v,u) with u > v searches v in u's prefix (a short
+// list after the degree relabel) and sets both directions; entries without a
+// reverse (asymmetric input) keep the 0xffffffff the array was filled with.
+template <int TILE>
+__global__ void __launch_bounds__(TILE) k_rev_build(const uint32_t *__restrict__ off,
+                                                    const uint32_t *__restrict__ tilerow,
+                                                    const int32_t *__restrict__ dst,
+                                                    const uint32_t *__restrict__ pre, uint32_t n, uint32_t m,
+                                                    uint32_t *__restrict__ rev) {
+  __shared__ accx_tile_rows<TILE> sh;
+  const uint32_t base = blockIdx.x * (uint32_t)TILE;
+  const uint32_t e = base + threadIdx.x;
+  const uint32_t v = accx_tile_row<TILE>(off, tilerow, n, m, base, e, &sh);
+  if (e >= m) return;
+  const uint32_t u = (uint32_t)dst[e];
+  if (u <= v) return;
+  const uint32_t ub = __ldg(off + u), ue = ub + __ldg(pre + u);
+  const uint32_t r = accx_lower_bound(dst, ub, ue, (int32_t)v);
+  if (r < ue && __ldg(dst + r) == (int32_t)v) {
+    rev[e] = r;
+    rev[r] = e;
+  }
+}
+
 // The two prefix ranges of an owned edge (x owner, y = dst[e]), each cut at
-// min(x, y): ids from there up cannot be common to both prefixes.
-__device__ __forceinline__ void accx_or_ranges(const uint32_t *__restrict__ off, const int32_t *__restrict__ dst,
-                                               const uint32_t *__restrict__ pre, uint32_t x, uint32_t y,
+// min(x, y): ids from there up cannot be common to both prefixes.  The cut of
+// P(x) at y < x is the entry e itself; the cut of P(y) at x < y is x's position
+// in N(y), the reverse entry.
+__device__ __forceinline__ void accx_or_ranges(const uint32_t *__restrict__ off, const uint32_t *__restrict__ pre,
+                                               const uint32_t *__restrict__ rev, uint32_t x, uint32_t y, uint32_t e,
                                                uint32_t *xb, uint32_t *xe, uint32_t *yb, uint32_t *ye) {
   *xb = __ldg(off + x);
   *xe = *xb + __ldg(pre + x);
   *yb = __ldg(off + y);
   *ye = *yb + __ldg(pre + y);
-  if (y < x) *xe = accx_lower_bound(dst, *xb, *xe, (int32_t)y);
-  else *ye = accx_lower_bound(dst, *yb, *ye, (int32_t)x);
+  if (y < x) {
+    *xe = min(*xe, e);
+  } else {
+    const uint32_t r = __ldg(rev + e);
+    *ye = (r >= *yb && r < *ye) ? r : *yb;
+  }
 }
 
 __global__ void __launch_bounds__(MERGE_WARPS * 32) k_merge_or(const uint32_t *__restrict__ off,
                                                                 const int32_t *__restrict__ dst,
                                                                 const uint32_t *__restrict__ pre,
+                                                                const uint32_t *__restrict__ rev,
                                                                 const uint2 *__restrict__ list, uint32_t list_cap,
                                                                 unsigned long long *__restrict__ ctr,
                                                                 int32_t *__restrict__ cnt) {
@@ -59,7 +91,7 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32) k_merge_or(const uint32_t *_
     const uint2 p = list[it];
     const uint32_t x = p.x, e = p.y, y = (uint32_t)__ldg(dst + e);
     uint32_t xb, xe, yb, ye;
-    accx_or_ranges(off, dst, pre, x, y, &xb, &xe, &yb, &ye);
+    accx_or_ranges(off, pre, rev, x, y, e, &xb, &xe, &yb, &ye);
     const uint32_t c = accx_warp_merge_credit(dst, xb, xe, yb, ye, buf[w][0], buf[w][1], lane, cnt);
     if (lane == 0 && c) atomicAdd(cnt + e, (int32_t)c);
     found += c;
@@ -73,6 +105,7 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32) k_merge_or(const uint32_t *_
 __global__ void __launch_bounds__(MERGE_WARPS * 32) k_gallop_or(const uint32_t *__restrict__ off,
                                                                  const int32_t *__restrict__ dst,
                                                                  const uint32_t *__restrict__ pre,
+                                                                 const uint32_t *__restrict__ rev,
                                                                  const uint2 *__restrict__ list, uint32_t list_cap,
                                                                  unsigned long long *__restrict__ ctr,
                                                                  int32_t *__restrict__ cnt) {
@@ -85,7 +118,7 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32) k_gallop_or(const uint32_t *
     const uint2 p = list[list_cap - 1 - it];
     const uint32_t x = p.x, e = p.y, y = (uint32_t)__ldg(dst + e);
     uint32_t xb, xe, yb, ye;
-    accx_or_ranges(off, dst, pre, x, y, &xb, &xe, &yb, &ye);
+    accx_or_ranges(off, pre, rev, x, y, e, &xb, &xe, &yb, &ye);
     uint32_t c = 0, lo = xb;
     for (uint32_t j0 = yb; j0 < ye && lo < xe; j0 += 32) {
       const uint32_t j = j0 + (uint32_t)lane;
@@ -109,56 +142,62 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32) k_gallop_or(const uint32_t *
   if (lane == 0 && found) atomicAdd(&ctr[C_MATCH + ACCX_KIND_GALLOP], found);
 }
 
-// Bitmap kind.  One CTA per work item (an owner x, or a slice of its list when
-// the owner's probe work is large).  The owner's prefix -- ids below x, which
-// the classifier keeps below W -- is staged as a dense bitmap over [0, W) plus,
-// per non-empty 32-bit word, the prefix position of the word's first id (rank of
-// an id = that base + popcount of the lower bits).  Then every owned entry
-// (x,y) of the slice probes P(y) cut at min(x,y): short probe lists are
-// concatenated across the CTA and streamed 32 ids per warp step, long ones are
-// pulled by whole warps with 16-byte loads.  A hit at partner entry j credits
-// cnt[j] (RED), the owner's shared counter of the id's rank, and the edge.
+// items[i] = the owner of bitmap work item i (items of one owner are contiguous).
+__global__ void k_item_fill(const unsigned long long *__restrict__ icnt, const unsigned long long *__restrict__ prefix,
+                            uint32_t n, uint32_t cap, uint32_t *__restrict__ items) {
+  for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
+    const unsigned long long c = icnt[u], p0 = prefix[u];
+    for (unsigned long long j = 0; j < c && p0 + j < cap; j++) items[p0 + j] = u;
+  }
+}
+
+#define SHORT_PIECE (32u * PROBE_UNROLL)  // ids per short piece (concatenated short lists)
+#define LONG_PIECE (32u * LONG_UNROLL)    // ids per piece of a long list
+
+// Bitmap kind.  CTAs take work items (an owner x, or a slice of its list when
+// the owner's probe work is large) from a device counter.  The owner's prefix
+// -- ids below x, which the classifier keeps below W -- is staged as a dense
+// bitmap over [0, W) plus, per non-empty 32-bit word, the prefix position of
+// the word's first id (rank of an id = that base + popcount of the lower bits).
+// The slice is walked in rounds of blockDim entries; the classifier stored, per
+// bitmap entry (x,y), where P(y) starts and its length cut at min(x,y) (0 for
+// other entries), so a round starts with one coalesced load per entry.  Short
+// probe lists are concatenated (CTA prefix sum); long ones are cut into pieces
+// of LONG_PIECE ids; warps take short chunks and long pieces from one shared
+// queue, so no warp waits behind one long list.  A hit at partner entry j
+// credits cnt[j] (RED), the owner's shared counter of the id's rank, and the
+// edge (shared per-entry counters, credited after the round).
 __global__ void __launch_bounds__(1024, 1) k_bitmap_or(const uint32_t *__restrict__ off,
                                                        const int32_t *__restrict__ dst,
-                                                       const uint32_t *__restrict__ pre, uint32_t n, int policy,
-                                                       const uint8_t *__restrict__ table,
+                                                       const uint32_t *__restrict__ pre, uint32_t n,
+                                                       const uint32_t *__restrict__ items, uint32_t items_cap,
                                                        const unsigned long long *__restrict__ work_u,
-                                                       const unsigned long long *__restrict__ prefix, uint32_t W,
-                                                       uint32_t pcap, uint32_t target, int32_t *__restrict__ cnt,
+                                                       const unsigned long long *__restrict__ prefix,
+                                                       const uint2 *__restrict__ sl, uint32_t W, uint32_t pcap,
+                                                       uint32_t target, int32_t *__restrict__ cnt,
                                                        unsigned long long *__restrict__ ctr) {
   extern __shared__ __align__(16) uint32_t smem[];
   const uint32_t nwords = W / 32;
   uint32_t *words = smem;                                          // nwords
   uint32_t *ocnt = smem + nwords;                                  // pcap owner-prefix counters
   uint16_t *wbase = reinterpret_cast<uint16_t *>(ocnt + pcap);     // nwords first-id positions
-  __shared__ uint8_t s_table[ACCX_NB * ACCX_NB];
-  __shared__ uint32_t s_u, s_tot, s_nseg, s_nlong, s_lnext;
-  __shared__ uint32_t s_wsum[32], s_wcnt[32], s_wlong[32];
+  __shared__ unsigned long long s_it;
+  __shared__ uint32_t s_tot, s_nseg, s_nlong, s_nlp, s_next;
+  __shared__ uint32_t s_wsum[32], s_wcnt[32], s_wlong[32], s_wlp[32];
   __shared__ uint32_t s_pre[1025], s_beg[1024], s_ent[1024], s_hit[1024];
-  __shared__ uint32_t s_lbeg[1024], s_llen[1024], s_lent[1024];
+  __shared__ uint32_t s_lbeg[1024], s_llen[1024], s_lent[1024], s_lpc[1025], s_lhit[1024];
   const int tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
-  for (int i = tid; i < ACCX_NB * ACCX_NB; i += nt) s_table[i] = table ? table[i] : 0;
   for (uint32_t i = tid; i < nwords; i += nt) words[i] = 0;
-  const unsigned long long total = prefix[n];
+  unsigned long long total = prefix[n];
+  if (total > items_cap) total = items_cap;
   unsigned long long found = 0, probed = 0;  // this thread's share, summed per warp at the end
+  if (tid == 0) s_it = atomicAdd(&ctr[C_ITEMS], 1ull);
   __syncthreads();
-  for (unsigned long long it = blockIdx.x; it < total; it += gridDim.x) {
-    if (warp == 0) {
-      uint32_t lo = 0, hi = n;
-      while (hi - lo > 1) {
-        uint32_t step = (hi - lo + 31) / 32;
-        uint32_t p = lo + (uint32_t)lane * step;
-        bool ok = p < hi && prefix[p] <= it;
-        unsigned b = __ballot_sync(ACCX_FULL_MASK, ok);
-        lo = lo + (31 - __clz(b)) * step;
-        uint32_t nh = lo + step;
-        hi = nh < hi ? nh : hi;
-      }
-      if (lane == 0) s_u = lo;
-    }
-    __syncthreads();
-    const uint32_t x = s_u;
+  for (;;) {
+    const unsigned long long it = s_it;
+    if (it >= total) break;
+    const uint32_t x = items[it];
     const uint32_t ub = off[x], ue = off[x + 1], du = ue - ub, px = pre[x];
     uint32_t nchunks, nsplit;
     accx_item_shape(du, 0, work_u[x], 1, target, &nchunks, &nsplit);
@@ -166,7 +205,6 @@ __global__ void __launch_bounds__(1024, 1) k_bitmap_or(const uint32_t *__restric
     const uint32_t pa = ub + (uint32_t)((unsigned long long)du * sp / nsplit);
     const uint32_t pb = ub + (uint32_t)((unsigned long long)du * (sp + 1) / nsplit);
     const uint32_t pxs = px <= pcap ? px : 0;  // the classifier guarantees px <= pcap for bitmap owners
-    // stage the prefix
     for (uint32_t i = tid; i < pxs; i += nt) {
       const uint32_t id = (uint32_t)__ldg(dst + ub + i);
       if (id < W) {
@@ -176,46 +214,49 @@ __global__ void __launch_bounds__(1024, 1) k_bitmap_or(const uint32_t *__restric
       ocnt[i] = 0;
     }
     __syncthreads();
+    if (tid == 0) s_it = atomicAdd(&ctr[C_ITEMS], 1ull);  // the next item, read after this one
     for (uint32_t r0 = pa; r0 < pb; r0 += (uint32_t)nt) {
       const uint32_t k = r0 + (uint32_t)tid;
       uint32_t sst = 0, len = 0;
       if (k < pb) {
-        const uint32_t y = (uint32_t)__ldg(dst + k);
-        const uint32_t py = __ldg(pre + y);
-        if (py > 0 && accx_owns(x, px, y, py) && accx_edge_kind(policy, s_table, px, py) == ACCX_KIND_BITMAP) {
-          sst = __ldg(off + y);
-          uint32_t t = sst + py;
-          if (y > x) t = accx_lower_bound(dst, sst, t, (int32_t)x);
-          len = t - sst;
-        }
+        const uint2 e = sl[k];
+        sst = e.x;
+        len = e.y;
       }
+      probed += len;
       const bool is_short = len > 0 && len < LONG_SEG, is_long = len >= LONG_SEG;
       const unsigned bs = __ballot_sync(ACCX_FULL_MASK, is_short), bl = __ballot_sync(ACCX_FULL_MASK, is_long);
-      const uint32_t slen = is_short ? len : 0u;
-      uint32_t incl = slen;
+      const uint32_t lp = is_long ? (len + LONG_PIECE - 1) / LONG_PIECE : 0u;
+      uint32_t incl = is_short ? len : 0u, lincl = lp;
 #pragma unroll
       for (int d = 1; d < 32; d <<= 1) {
-        uint32_t v = __shfl_up_sync(ACCX_FULL_MASK, incl, d);
-        if (lane >= d) incl += v;
+        const uint32_t a = __shfl_up_sync(ACCX_FULL_MASK, incl, d), b = __shfl_up_sync(ACCX_FULL_MASK, lincl, d);
+        if (lane >= d) { incl += a; lincl += b; }
       }
       if (lane == 31) {
         s_wsum[warp] = incl;
         s_wcnt[warp] = __popc(bs);
         s_wlong[warp] = __popc(bl);
+        s_wlp[warp] = lincl;
       }
       __syncthreads();
       if (warp == 0) {
-        uint32_t ws = lane < nwarps ? s_wsum[lane] : 0u, wc = lane < nwarps ? s_wcnt[lane] : 0u;
-        uint32_t wl = lane < nwarps ? s_wlong[lane] : 0u;
-        uint32_t is = ws, ic = wc, il = wl;
+        const uint32_t ws = lane < nwarps ? s_wsum[lane] : 0u, wc = lane < nwarps ? s_wcnt[lane] : 0u;
+        const uint32_t wl = lane < nwarps ? s_wlong[lane] : 0u, wp = lane < nwarps ? s_wlp[lane] : 0u;
+        uint32_t is = ws, ic = wc, il = wl, ip = wp;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
-          uint32_t a = __shfl_up_sync(ACCX_FULL_MASK, is, d), b = __shfl_up_sync(ACCX_FULL_MASK, ic, d);
-          uint32_t q = __shfl_up_sync(ACCX_FULL_MASK, il, d);
-          if (lane >= d) { is += a; ic += b; il += q; }
+          const uint32_t a = __shfl_up_sync(ACCX_FULL_MASK, is, d), b = __shfl_up_sync(ACCX_FULL_MASK, ic, d);
+          const uint32_t c = __shfl_up_sync(ACCX_FULL_MASK, il, d), q = __shfl_up_sync(ACCX_FULL_MASK, ip, d);
+          if (lane >= d) { is += a; ic += b; il += c; ip += q; }
         }
-        if (lane < nwarps) { s_wsum[lane] = is - ws; s_wcnt[lane] = ic - wc; s_wlong[lane] = il - wl; }
-        if (lane == 31) { s_tot = is; s_nseg = ic; s_nlong = il; s_lnext = 0; }
+        if (lane < nwarps) {
+          s_wsum[lane] = is - ws;
+          s_wcnt[lane] = ic - wc;
+          s_wlong[lane] = il - wl;
+          s_wlp[lane] = ip - wp;
+        }
+        if (lane == 31) { s_tot = is; s_nseg = ic; s_nlong = il; s_nlp = ip; s_next = 0; }
       }
       __syncthreads();
       if (is_short) {
@@ -230,71 +271,86 @@ __global__ void __launch_bounds__(1024, 1) k_bitmap_or(const uint32_t *__restric
         s_lbeg[idx] = sst;
         s_llen[idx] = len;
         s_lent[idx] = k;
+        s_lpc[idx] = s_wlp[warp] + lincl - lp;
+        s_lhit[idx] = 0;
+      }
+      if (tid == 0) {
+        s_pre[s_nseg] = s_tot;
+        s_lpc[s_nlong] = s_nlp;
       }
       __syncthreads();
       const uint32_t tot = s_tot, nseg = s_nseg, nlong = s_nlong;
-      if (tid == 0) s_pre[nseg] = tot;
-      probed += len;
-      __syncthreads();
-      // short parts
-      for (uint32_t c0 = (uint32_t)warp * 32u * PROBE_UNROLL; c0 < tot; c0 += (uint32_t)nwarps * 32u * PROBE_UNROLL) {
-        uint32_t lo = 0, hi = nseg;
-        while (hi - lo > 1) {
-          uint32_t step = (hi - lo + 31) / 32;
-          uint32_t p = lo + (uint32_t)lane * step;
-          unsigned b = __ballot_sync(ACCX_FULL_MASK, p < hi && s_pre[p] <= c0);
-          lo += (31 - __clz(b)) * step;
-          uint32_t nh = lo + step;
-          hi = nh < hi ? nh : hi;
-        }
-        uint32_t segb = lo;
-        int32_t xs[PROBE_UNROLL];
-        uint32_t sg[PROBE_UNROLL], gi[PROBE_UNROLL];
+      const uint32_t nsp = (tot + SHORT_PIECE - 1) / SHORT_PIECE, npieces = nsp + s_nlp;
+      for (;;) {
+        uint32_t p = 0;
+        if (lane == 0) p = atomicAdd(&s_next, 1u);
+        p = __shfl_sync(ACCX_FULL_MASK, p, 0);
+        if (p >= npieces) break;
+        if (p < nsp) {
+          // short chunk: SHORT_PIECE consecutive ids of the concatenation
+          const uint32_t c0 = p * SHORT_PIECE;
+          uint32_t lo = 0, hi = nseg;
+          while (hi - lo > 1) {
+            const uint32_t step = (hi - lo + 31) / 32;
+            const uint32_t q = lo + (uint32_t)lane * step;
+            const unsigned b = __ballot_sync(ACCX_FULL_MASK, q < hi && s_pre[q] <= c0);
+            lo += (31 - __clz(b)) * step;
+            const uint32_t nh = lo + step;
+            hi = nh < hi ? nh : hi;
+          }
+          uint32_t segb = lo;
+          int32_t xs[PROBE_UNROLL];
+          uint32_t sg[PROBE_UNROLL], gi[PROBE_UNROLL];
 #pragma unroll
-        for (int r = 0; r < PROBE_UNROLL; r++) {
-          const uint32_t i0 = c0 + 32u * r;
-          const uint32_t i = i0 + (uint32_t)lane;
-          const uint32_t kb = segb + 1u + (uint32_t)lane;
-          const uint32_t bnd = kb <= nseg ? s_pre[kb] : 0xffffffffu;
-          const uint32_t o = bnd - i0;
-          const unsigned M = __reduce_or_sync(ACCX_FULL_MASK, o < 32u ? (1u << o) : 0u);
-          const uint32_t sj = segb + __popc(M & (lane == 31 ? 0xffffffffu : ((2u << lane) - 1u)));
-          sg[r] = sj;
-          gi[r] = (i < tot) ? s_beg[sj] + (i - s_pre[sj]) : 0u;
-          xs[r] = (i < tot) ? __ldg(dst + gi[r]) : -1;
-          segb += __popc(M) + (__ballot_sync(ACCX_FULL_MASK, o == 32u) ? 1u : 0u);
-        }
+          for (int r = 0; r < PROBE_UNROLL; r++) {
+            const uint32_t i0 = c0 + 32u * r;
+            const uint32_t i = i0 + (uint32_t)lane;
+            const uint32_t kb = segb + 1u + (uint32_t)lane;
+            const uint32_t bnd = kb <= nseg ? s_pre[kb] : 0xffffffffu;
+            const uint32_t o = bnd - i0;
+            const unsigned M = __reduce_or_sync(ACCX_FULL_MASK, o < 32u ? (1u << o) : 0u);
+            const uint32_t sj = segb + __popc(M & (lane == 31 ? 0xffffffffu : ((2u << lane) - 1u)));
+            sg[r] = sj;
+            gi[r] = (i < tot) ? s_beg[sj] + (i - s_pre[sj]) : 0u;
+            xs[r] = (i < tot) ? __ldg(dst + gi[r]) : -1;
+            segb += __popc(M) + (__ballot_sync(ACCX_FULL_MASK, o == 32u) ? 1u : 0u);
+          }
 #pragma unroll
-        for (int r = 0; r < PROBE_UNROLL; r++) {
-          const uint32_t id = (uint32_t)xs[r];
-          if (xs[r] >= 0 && id < W) {
-            const uint32_t wd = words[id >> 5], bit = 1u << (id & 31);
-            if (wd & bit) {
-              const uint32_t rk = wbase[id >> 5] + __popc(wd & (bit - 1u));
-              atomicAdd(cnt + gi[r], 1);
-              if (rk < pxs) atomicAdd(&ocnt[rk], 1u);  // always true on a sorted CSR
-              atomicAdd(&s_hit[sg[r]], 1u);
+          for (int r = 0; r < PROBE_UNROLL; r++) {
+            const uint32_t id = (uint32_t)xs[r];
+            if (xs[r] >= 0 && id < W) {
+              const uint32_t wd = words[id >> 5], bit = 1u << (id & 31);
+              if (wd & bit) {
+                const uint32_t rk = wbase[id >> 5] + __popc(wd & (bit - 1u));
+                atomicAdd(cnt + gi[r], 1);
+                if (rk < pxs) atomicAdd(&ocnt[rk], 1u);  // always true on a sorted CSR
+                atomicAdd(&s_hit[sg[r]], 1u);
+              }
             }
           }
-        }
-      }
-      // long parts
-      for (;;) {
-        uint32_t q = 0;
-        if (lane == 0) q = atomicAdd(&s_lnext, 1u);
-        q = __shfl_sync(ACCX_FULL_MASK, q, 0);
-        if (q >= nlong) break;
-        const uint32_t a0 = s_lbeg[q], a1 = a0 + s_llen[q];
-        uint32_t h = 0;
-        // lane-consecutive ids, LONG_UNROLL loads in flight per lane: a warp's
-        // credits for one load land in one 128-byte line of cnt
-        for (uint32_t j0 = a0; j0 < a1; j0 += 32u * LONG_UNROLL) {
+        } else {
+          // a piece of a long list: lane-consecutive ids, LONG_UNROLL loads in
+          // flight per lane; a warp's credits for one load land in one line of cnt
+          const uint32_t pl = p - nsp;
+          uint32_t lo = 0, hi = nlong;
+          while (hi - lo > 1) {
+            const uint32_t step = (hi - lo + 31) / 32;
+            const uint32_t q = lo + (uint32_t)lane * step;
+            const unsigned b = __ballot_sync(ACCX_FULL_MASK, q < hi && s_lpc[q] <= pl);
+            lo += (31 - __clz(b)) * step;
+            const uint32_t nh = lo + step;
+            hi = nh < hi ? nh : hi;
+          }
+          const uint32_t q = lo;
+          const uint32_t a1 = s_lbeg[q] + s_llen[q];
+          const uint32_t j0 = s_lbeg[q] + (pl - s_lpc[q]) * LONG_PIECE;
           int32_t v[LONG_UNROLL];
 #pragma unroll
           for (int r = 0; r < LONG_UNROLL; r++) {
             const uint32_t j = j0 + 32u * r + (uint32_t)lane;
             v[r] = j < a1 ? __ldg(dst + j) : -1;
           }
+          uint32_t h = 0;
 #pragma unroll
           for (int r = 0; r < LONG_UNROLL; r++) {
             const uint32_t id = (uint32_t)v[r];
@@ -308,18 +364,16 @@ __global__ void __launch_bounds__(1024, 1) k_bitmap_or(const uint32_t *__restric
               }
             }
           }
-        }
-        h = __reduce_add_sync(ACCX_FULL_MASK, h);
-        if (lane == 0) found += h;
-        if (lane == 0 && h) {
-          const uint32_t kk = s_lent[q];
-          if (kk - ub < pxs) atomicAdd(&ocnt[kk - ub], h);
-          else atomicAdd(cnt + kk, (int32_t)h);
+          h = __reduce_add_sync(ACCX_FULL_MASK, h);
+          if (lane == 0 && h) atomicAdd(&s_lhit[q], h);
         }
       }
       __syncthreads();
-      for (uint32_t q = tid; q < nseg; q += nt) {
-        const uint32_t h = s_hit[q], kk = s_ent[q];
+      // edge credits: the entry itself when it lies in x's prefix goes to the
+      // owner's counters, else straight to HBM
+      for (uint32_t q = tid; q < nseg + nlong; q += nt) {
+        const bool sh = q < nseg;
+        const uint32_t h = sh ? s_hit[q] : s_lhit[q - nseg], kk = sh ? s_ent[q] : s_lent[q - nseg];
         found += h;
         if (h) {
           if (kk - ub < pxs) atomicAdd(&ocnt[kk - ub], h);
@@ -356,28 +410,17 @@ __global__ void __launch_bounds__(1024, 1) k_bitmap_or(const uint32_t *__restric
 }
 
 // Sum of the two entries of every undirected edge, plus the bias, into both.
-// One thread per suffix entry e = (v,u), u > v; the other entry is v's position
-// in u's prefix, a short list (at most sqrt(2m) ids after the degree relabel),
-// where the reverse search from a prefix entry would walk a hub's long suffix.
-template <int TILE>
-__global__ void __launch_bounds__(TILE) k_combine_or(const uint32_t *__restrict__ off,
-                                                     const uint32_t *__restrict__ tilerow,
-                                                     const int32_t *__restrict__ dst,
-                                                     const uint32_t *__restrict__ pre, uint32_t n, uint32_t m,
-                                                     int32_t bias, int32_t *__restrict__ cnt) {
-  __shared__ accx_tile_rows<TILE> sh;
-  const uint32_t base = blockIdx.x * (uint32_t)TILE;
-  const uint32_t e = base + threadIdx.x;
-  const uint32_t v = accx_tile_row<TILE>(off, tilerow, n, m, base, e, &sh);
-  if (e >= m) return;
-  const uint32_t u = (uint32_t)dst[e];
-  if (u <= v) return;
-  const uint32_t ub = __ldg(off + u), ue = ub + __ldg(pre + u);
-  const uint32_t r = accx_lower_bound(dst, ub, ue, (int32_t)v);
-  int32_t c = cnt[e] + bias;
-  if (r < ue && __ldg(dst + r) == (int32_t)v) {
-    c += cnt[r];
-    cnt[r] = c;
+// A pair is handled from its lower entry (v,u), u > v, whose rev is the higher
+// one; an entry without a reverse (asymmetric input) just gets the bias.
+__global__ void k_combine_or(uint32_t m, const uint32_t *__restrict__ rev, int32_t bias, int32_t *__restrict__ cnt) {
+  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < m; e += gridDim.x * blockDim.x) {
+    const uint32_t r = rev[e];
+    if (r < e) continue;
+    int32_t c = cnt[e] + bias;
+    if (r != 0xffffffffu) {
+      c += cnt[r];
+      cnt[r] = c;
+    }
+    cnt[e] = c;
   }
-  cnt[e] = c;
 }

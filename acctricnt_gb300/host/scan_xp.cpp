@@ -51,9 +51,12 @@ ScanXpOptions ScanXpOptions::from_env() {
     else if (s == "bitmap") o.policy = ACCX_POLICY_BITMAP;
     else if (s == "model") o.policy = ACCX_POLICY_MODEL;
     else o.policy = ACCX_POLICY_TABLE;
+    o.policy_set = true;
   }
   const char *r = getenv("ACCX_RELABEL");
   if (r) o.relabel = atoi(r) != 0;
+  const char *q = getenv("ACCX_ORIENT");
+  if (q) o.orient = atoi(q) != 0;
   return o;
 }
 
@@ -102,10 +105,14 @@ void SCAN_XP::CheckCore() {
   o.table = table;
   o.bias = 2;  // common_node_num = 2 + |N(u) ∩ N(v)|
   o.block_warps = opts_.block_warps;
+  o.orient = opts_.orient ? 1 : 0;
+  // oriented counts without a chosen policy: the bitmap kind for every edge, the
+  // fastest fixed choice on skewed graphs (owners past the window fall back to merge)
+  if (opts_.orient && !opts_.policy_set && o.policy == ACCX_POLICY_TABLE) o.policy = ACCX_POLICY_BITMAP;
   auto t0 = clk::now();
   check(accx_cn_count(g_, &o, nullptr, nullptr), "count");
   check(accx_scan_query(g_, epsilon_, min_u_, nullptr, nullptr, nullptr, &summary, nullptr), "similarity");
-  accx_log("All-Edge CN-Cnt + core checking (GPU): %.3lf s", secs(t0));
+  accx_log("All-Edge CN-Cnt + core checking (GPU, %s): %.3lf s", opts_.orient ? "oriented" : "direct", secs(t0));
 }
 
 void SCAN_XP::ClusterCore() {

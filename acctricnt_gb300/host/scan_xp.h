@@ -16,9 +16,12 @@
 
 struct ScanXpOptions {
   int policy = ACCX_POLICY_TABLE;  // counting policy (ACCX_POLICY_*); TABLE uses the default bucket table
+  bool policy_set = false;         // policy chosen by the caller (else oriented counts use the bitmap kind)
   bool relabel = true;             // count on the degree-descending relabeled copy
+  bool orient = true;              // oriented counting (triangle credits on prefix lists; same counts)
   int block_warps = 0;             // bitmap/merge CTA size in warps (0 = default)
-  static ScanXpOptions from_env(); // ACCX_POLICY=heuristic|merge|gallop|bitmap|table|model, ACCX_RELABEL=0|1
+  // ACCX_POLICY=heuristic|merge|gallop|bitmap|table|model, ACCX_RELABEL=0|1, ACCX_ORIENT=0|1
+  static ScanXpOptions from_env();
 };
 
 class SCAN_XP {

@@ -22,7 +22,7 @@ def test_cli_usage_and_missing_graph(tmp_path):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", golden_cases())
-@pytest.mark.parametrize("variant", ["plain", "varying", "heuristic_norelabel"])
+@pytest.mark.parametrize("variant", ["plain", "varying", "heuristic_norelabel", "direct"])
 def test_cli_result_file_matches_reference(name, variant, tmp_path):
     g = load_golden(name)
     d = str(tmp_path)
@@ -35,6 +35,8 @@ def test_cli_result_file_matches_reference(name, variant, tmp_path):
         cmd = [CLI, d, eps, mu, "4", os.path.join(d, "log.txt")]
     if variant == "heuristic_norelabel":
         env.update(ACCX_POLICY="heuristic", ACCX_RELABEL="0")
+    if variant == "direct":  # the reference's formulation: full-list intersections
+        env.update(ACCX_ORIENT="0")
     r = subprocess.run(cmd, capture_output=True, text=True, env=env)
     assert r.returncode == 0, r.stderr
     with open(os.path.join(d, str(g["result_name"])), "rb") as f:

@@ -71,6 +71,10 @@ __global__ void __launch_bounds__(TILE) k_classify(const uint32_t *__restrict__ 
                                                    const uint32_t *__restrict__ rev) {
   __shared__ accx_tile_rows<TILE> sh;
   __shared__ uint8_t s_table[ACCX_NB * ACCX_NB];
+  // per-kind edges / work / owner-side sums of this CTA, added to the device
+  // counters once per CTA (per-warp atomics on the same few words serialise in L2)
+  __shared__ unsigned long long s_st[3 * ACCX_NUM_KINDS];
+  if (threadIdx.x < 3 * ACCX_NUM_KINDS) s_st[threadIdx.x] = 0;
   if (policy == ACCX_POLICY_TABLE || policy == ACCX_POLICY_MODEL)
     for (int i = threadIdx.x; i < ACCX_NB * ACCX_NB; i += TILE) s_table[i] = table[i];
   uint32_t base = blockIdx.x * (uint32_t)TILE;
@@ -123,9 +127,9 @@ __global__ void __launch_bounds__(TILE) k_classify(const uint32_t *__restrict__ 
     int leader = __ffs(mask) - 1;
     unsigned long long basepos = 0;
     if (lane == leader) {
-      atomicAdd(&ctr[C_EDGES + k], (unsigned long long)__popc(mask));
-      atomicAdd(&ctr[C_WORK + k], w);
-      if (wo) atomicAdd(&ctr[C_OWNER + k], wo);
+      atomicAdd(&s_st[k], (unsigned long long)__popc(mask));
+      atomicAdd(&s_st[ACCX_NUM_KINDS + k], w);
+      if (wo) atomicAdd(&s_st[2 * ACCX_NUM_KINDS + k], wo);
       if (k == ACCX_KIND_MERGE) basepos = atomicAdd(&ctr[C_MERGE], (unsigned long long)__popc(mask));
       if (k == ACCX_KIND_GALLOP) basepos = atomicAdd(&ctr[C_GALLOP], (unsigned long long)__popc(mask));
     }
@@ -147,6 +151,9 @@ __global__ void __launch_bounds__(TILE) k_classify(const uint32_t *__restrict__ 
       if (lane == __ffs(peers) - 1) atomicAdd(&work_u[u], (unsigned long long)sw + 1ull);
     }
   }
+  static_assert(C_WORK == C_EDGES + ACCX_NUM_KINDS && C_OWNER == C_WORK + ACCX_NUM_KINDS, "counter layout");
+  __syncthreads();
+  if (threadIdx.x < 3 * ACCX_NUM_KINDS && s_st[threadIdx.x]) atomicAdd(&ctr[C_EDGES + threadIdx.x], s_st[threadIdx.x]);
 }
 
 // ---------------------------------------------------------------------------
@@ -655,7 +662,7 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s)
   unsigned long long *ctr = g->d_counters;
   unsigned long long *work_u = g->d_counters + C_NUM;
   ACCX_CUDA_TRY(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long) * (C_NUM + (size_t)n + 1), s));
-  ACCX_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (size_t)(m ? m : 1), s));
+  if (!orient) ACCX_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (size_t)(m ? m : 1), s));
   if (m == 0) {
     g->cnt_bias = bias;
     g->cnt_valid = true;
@@ -688,6 +695,7 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s)
       g->rev_csr = nullptr;
       if (g->home) ACCX_CUDA_TRY(cudaStreamSynchronize(g->home));
     }
+    k_fill<<<sms * 8, 256, 0, s>>>(cnt, m, bias);
     k_pre<<<sms * 8, 256, 0, s>>>(off, dst, n, g->d_pre);
     // reverse entries: built on the first oriented count of this CSR and kept
     // (an index of the graph, like the tile rows)
@@ -716,7 +724,7 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s)
     k_bitmap_or<<<sms * per_sm, warps * 32, smem, s>>>(off, dst, g->d_pre, n, g->d_or_items, items_cap, work_u,
                                                        g->d_prefix, g->d_or_sl, W, pcap, target, cnt, ctr);
     ACCX_MARK(4);
-    k_combine_or<<<sms * 8, 256, 0, s>>>(m, g->d_rev, bias, cnt);
+    k_combine_or<<<tiles, 256, 0, s>>>(m, g->d_rev, cnt);
   } else {
     k_classify<256, false><<<tiles, 256, 0, s>>>(off, tilerow, dst, n, m, policy, g->d_table, g->d_edge_list, list_cap,
                                                  work_u, ctr, nullptr, 0u, 0u, nullptr, nullptr);

@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32) k_merge_or(const uint32_t *_
     uint32_t xb, xe, yb, ye;
     accx_or_ranges(off, pre, rev, x, y, e, &xb, &xe, &yb, &ye);
     const uint32_t c = accx_warp_merge_credit(dst, xb, xe, yb, ye, buf[w][0], buf[w][1], lane, cnt);
-    if (lane == 0 && c) atomicAdd(cnt + e, (int32_t)c);
+    if (lane == 0 && c) atomicAdd(cnt + (y < x ? e : ye), (int32_t)c);  // the edge's prefix entry
     found += c;
     __syncwarp();
   }
@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32) k_gallop_or(const uint32_t *
       lo = __shfl_sync(ACCX_FULL_MASK, pos, (int)last_lane);
     }
     c = __reduce_add_sync(ACCX_FULL_MASK, c);
-    if (lane == 0 && c) atomicAdd(cnt + e, (int32_t)c);
+    if (lane == 0 && c) atomicAdd(cnt + (y < x ? e : ye), (int32_t)c);  // the edge's prefix entry
     found += c;
   }
   if (lane == 0 && found) atomicAdd(&ctr[C_MATCH + ACCX_KIND_GALLOP], found);
@@ -369,15 +369,21 @@ __global__ void __launch_bounds__(1024, 1) k_bitmap_or(const uint32_t *__restric
         }
       }
       __syncthreads();
-      // edge credits: the entry itself when it lies in x's prefix goes to the
-      // owner's counters, else straight to HBM
+      // edge credits go to the edge's prefix entry: the entry itself when y < x
+      // (through the owner's counters), else x's position in N(y), which is where
+      // the partner range was cut
       for (uint32_t q = tid; q < nseg + nlong; q += nt) {
         const bool sh = q < nseg;
         const uint32_t h = sh ? s_hit[q] : s_lhit[q - nseg], kk = sh ? s_ent[q] : s_lent[q - nseg];
         found += h;
         if (h) {
-          if (kk - ub < pxs) atomicAdd(&ocnt[kk - ub], h);
-          else atomicAdd(cnt + kk, (int32_t)h);
+          if (kk - ub < px) {
+            if (kk - ub < pxs) atomicAdd(&ocnt[kk - ub], h);
+            else atomicAdd(cnt + kk, (int32_t)h);
+          } else {
+            const uint32_t cut = sh ? s_beg[q] + (s_pre[q + 1] - s_pre[q]) : s_lbeg[q - nseg] + s_llen[q - nseg];
+            atomicAdd(cnt + cut, (int32_t)h);
+          }
         }
       }
       __syncthreads();
@@ -409,18 +415,18 @@ __global__ void __launch_bounds__(1024, 1) k_bitmap_or(const uint32_t *__restric
   }
 }
 
-// Sum of the two entries of every undirected edge, plus the bias, into both.
-// A pair is handled from its lower entry (v,u), u > v, whose rev is the higher
-// one; an entry without a reverse (asymmetric input) just gets the bias.
-__global__ void k_combine_or(uint32_t m, const uint32_t *__restrict__ rev, int32_t bias, int32_t *__restrict__ cnt) {
-  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < m; e += gridDim.x * blockDim.x) {
-    const uint32_t r = rev[e];
-    if (r < e) continue;
-    int32_t c = cnt[e] + bias;
-    if (r != 0xffffffffu) {
-      c += cnt[r];
-      cnt[r] = c;
-    }
-    cnt[e] = c;
-  }
+// Every credit lands on an edge's prefix entry (the entry in the larger id's
+// list), which starts at the bias; the other entry copies it.
+__global__ void k_fill(int32_t *__restrict__ cnt, uint32_t m, int32_t v) {
+  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < m; e += gridDim.x * blockDim.x) cnt[e] = v;
+}
+
+// One thread per entry: a suffix entry e = (v,u), u > v, takes the count of its
+// reverse rev[e] > e (u's prefix entry); entries without a reverse (asymmetric
+// input) keep the bias.
+__global__ void k_combine_or(uint32_t m, const uint32_t *__restrict__ rev, int32_t *__restrict__ cnt) {
+  const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m) return;
+  const uint32_t r = rev[e];
+  if (r != 0xffffffffu && r > e) cnt[e] = cnt[r];
 }

@@ -19,7 +19,7 @@
 // Included by count.cu after the shared counting definitions.
 #pragma once
 
-#define LONG_UNROLL 8  // loads in flight per lane on long probe lists
+#define LONG_UNROLL 16  // loads in flight per lane on long probe lists (8 measured 4% slower, 4 25% slower)
 
 // pre[u] = |N(u) ∩ [0, u)|.
 __global__ void k_pre(const uint32_t *__restrict__ off, const int32_t *__restrict__ dst, uint32_t n,

@@ -140,7 +140,7 @@ def collect(graph_params, reps=2, relabel=True, log=None, orient=False):
 
 
 def calibration_graphs():
-    return training_graphs() + [accx.rmat_params(20, 16, seed=18)]
+    return training_graphs() + [accx.rmat_params(20, 16, seed=18), accx.rmat_params(22, 16, seed=19)]
 
 
 BITMAP_OFFSETS = (0.0, -0.5, -1.0, -1.5, -2.0, -3.0, -5.0, -64.0)
@@ -149,24 +149,49 @@ BITMAP_OFFSETS = (0.0, -0.5, -1.0, -1.5, -2.0, -3.0, -5.0, -64.0)
 def calibrate(model, graph_params, orient=False, reps=3, offsets=BITMAP_OFFSETS, log=None):
     """Fits the bitmap kind's log2 offset on whole counts: for every candidate
     offset the model's table is run as a whole count on every calibration graph
-    (relabeled), and the offset with the smallest sum of times relative to each
-    graph's best candidate is kept (ties: the smaller offset).  -64 amounts to
-    the bitmap kind for every bucket."""
+    (relabeled), and the offset with the smallest size-weighted mean of times
+    relative to each graph's best candidate is kept (ties: the smaller offset);
+    a graph's weight is its share of the calibration set's CSR entries, so the
+    large graphs decide.  -64 amounts to the bitmap kind for every bucket."""
     rel = np.zeros((len(graph_params), len(offsets)))
+    wts = np.zeros(len(graph_params))
     for gi, p in enumerate(graph_params):
         G = accx.Graph.generate(p)
         G.relabel()
+        wts[gi] = G.m
         for ci, off in enumerate(offsets):
             model.set_kind_bias([0.0, 0.0, off])
             rel[gi, ci] = _count_phase_ms(G, model.table_for(G, orient).reshape(-1), reps, None, orient)
         G.free()
-    score = (rel / rel.min(1, keepdims=True)).sum(0)
+    wts = wts / max(wts.sum(), 1.0)
+    score = ((rel / rel.min(1, keepdims=True)) * wts[:, None]).sum(0) * len(graph_params)
     best = int(np.argmin(score))
     model.set_kind_bias([0.0, 0.0, offsets[best]])
     if log:
         log("calibrated bitmap offset %.2f (scores %s)" % (offsets[best], np.round(score, 3).tolist()))
     return {"kind_bias": [0.0, 0.0, float(offsets[best])], "offsets": list(offsets),
             "relative_time": [round(float(v) / len(graph_params), 4) for v in score]}
+
+
+def tune_offset(G, model, orient=False, reps=2, offsets=BITMAP_OFFSETS, stream=None):
+    """Refines the bitmap offset on the graph about to be counted: each candidate
+    offset's model table runs once as a whole count (best of `reps`), and the
+    fastest is kept in the model (ties: the calibrated offset).  The model still
+    orders the kinds of every bucket; only the one trade-off scalar, which
+    depends on the graph's scale, is measured in place -- as the launch-shape
+    autotuner does for the bitmap kernel's shape."""
+    t0 = time.perf_counter()
+    base = float(model.kind_bias()[2])
+    ms = []
+    for off in offsets:
+        model.set_kind_bias([0.0, 0.0, off])
+        ms.append(_count_phase_ms(G, model.table_for(G, orient).reshape(-1), reps, stream, orient))
+    best = int(np.argmin(ms))
+    if base in offsets and ms[offsets.index(base)] <= ms[best]:
+        best = offsets.index(base)
+    model.set_kind_bias([0.0, 0.0, offsets[best]])
+    return {"kind_bias": [0.0, 0.0, float(offsets[best])], "calibrated_offset": base,
+            "candidate_ms": [round(float(v), 3) for v in ms], "seconds": round(time.perf_counter() - t0, 2)}
 
 
 def train_default(seed=1, epochs=4000, lr=3e-3, log=None, orient=False, calibrate_bias=True):

@@ -156,6 +156,8 @@ def pick_policy(G, args):
     pl = sched.plan(G, md, mo)
     info = {"direct_model": dict(info_d), "oriented_model": dict(info_o), "plan": pl,
             "model_ready_s": round(time.perf_counter() - t0, 2)}
+    # the chosen mode's bitmap offset, refined on this graph (preprocessing, like the relabel)
+    info["offset_tune"] = sched.tune_offset(G, mo if pl["orient"] else md, orient=bool(pl["orient"]))
     return "model", bool(pl["orient"]), {False: md, True: mo}, info
 
 

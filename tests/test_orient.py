@@ -162,3 +162,17 @@ def test_kind_bias_steers_the_table():
     assert np.array_equal(G.count(policy="model", orient=True), ref)
     with pytest.raises(accx.AccxError):
         m.set_kind_bias([0.0, float("nan"), 0.0])
+
+
+def test_tune_offset_keeps_a_candidate_and_counts_stay_exact():
+    from acctricnt_gb300 import sched
+    m = accx.Model(seed=9)
+    G = accx.Graph.generate(accx.rmat_params(15, 16, seed=6))
+    ref = G.count(policy="heuristic")
+    G.relabel()
+    info = sched.tune_offset(G, m, orient=True, reps=1)
+    assert len(info["candidate_ms"]) == len(sched.BITMAP_OFFSETS)
+    assert info["kind_bias"][2] in sched.BITMAP_OFFSETS
+    assert np.isclose(m.kind_bias()[2], info["kind_bias"][2])
+    G.set_model(m, orient=True)
+    assert np.array_equal(G.count(policy="model", orient=True), ref)

@@ -76,7 +76,7 @@ class Result(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("workers", C.c_int), ("hbm_budget", C.c_uint64), ("count_policy", C.c_int),
-                ("count_sm_percent", C.c_int)]
+                ("count_sm_percent", C.c_int), ("count_orient", C.c_int)]
 
 
 class ServerStats(C.Structure):
@@ -422,9 +422,9 @@ class Graph:
         _check(lib.accx_cn_last_timings(self._h, _ptr(ms)), "cn_last_timings")
         return dict(zip(PHASES, (float(x) for x in ms)))
 
-    def autotune(self, policy="bitmap", reps=2, stream=None):
+    def autotune(self, policy="bitmap", reps=2, stream=None, orient=False):
         """Fastest bitmap-kernel launch shape for `policy`; returns (kwargs, ms, all_ms)."""
-        base, keep = self._opts(policy, None, 0, 0, 0)
+        base, keep = self._opts(policy, None, 0, 0, 0, False, 0, orient)
         best = CountOpts()
         bms = C.c_float()
         allms = np.zeros(16, np.float32)
@@ -584,7 +584,7 @@ class Batch:
 
     def capture(self, policy="model", bias=0, stream=None, **kw):
         opts, keep = Graph._opts(policy, None, bias, kw.get("block_warps", 0), kw.get("window_kb", 0), False,
-                                 kw.get("sparse_kb", 0))
+                                 kw.get("sparse_kb", 0), kw.get("orient", False))
         _check(lib.accx_batch_capture(self._h, C.byref(opts), _stream_ptr(stream)), "batch_capture")
 
     def launch(self, stream=None):
@@ -610,10 +610,11 @@ class Server:
     """accx_server: continuous batching of SCAN queries on a resident counted
     graph and of new-graph count requests, admitted by an HBM budget."""
 
-    def __init__(self, resident, workers=4, hbm_budget=0, count_policy="bitmap", count_sm_percent=0):
+    def __init__(self, resident, workers=4, hbm_budget=0, count_policy="bitmap", count_sm_percent=0,
+                 count_orient=False):
         self.resident = resident
         pol = POLICIES[count_policy] if isinstance(count_policy, str) else int(count_policy)
-        cfg = ServerConfig(int(workers), int(hbm_budget), pol, int(count_sm_percent))
+        cfg = ServerConfig(int(workers), int(hbm_budget), pol, int(count_sm_percent), 1 if count_orient else 0)
         self._h = C.c_void_p()
         _check(lib.accx_server_create(resident._h, C.byref(cfg), C.byref(self._h)), "server_create")
 

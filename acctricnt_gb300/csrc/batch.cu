@@ -176,9 +176,13 @@ extern "C" int accx_batch_launch(accx_batch *b, void *stream) {
 extern "C" int accx_autotune(accx_graph *g, const accx_count_opts *base, int reps, accx_count_opts *best,
                              float *best_ms, float *all_ms, int *ncand, void *stream) {
   if (!g || !best || reps < 1) return ACCX_ERR_INVALID_ARG;
-  static const int cands[][3] = {  // block warps, dense KiB, sparse KiB
+  static const int cands_direct[][3] = {  // block warps, dense KiB, sparse KiB
       {32, 128, 64}, {32, 160, 32}, {32, 96, 96}, {32, 64, 64}, {16, 128, 64}, {16, 48, 32}, {24, 128, 64}};
-  const int nc = (int)(sizeof(cands) / sizeof(cands[0]));
+  static const int cands_orient[][3] = {  // block warps, dense KiB, owner-counter KiB
+      {32, 64, 16}, {32, 48, 16}, {32, 80, 16}, {32, 96, 16}, {32, 64, 8}, {16, 32, 16}, {24, 64, 16}};
+  const bool orient = base && base->orient;
+  const int(*cands)[3] = orient ? cands_orient : cands_direct;
+  const int nc = 7;
   cudaStream_t s = (cudaStream_t)stream;
   cudaEvent_t e0, e1;
   ACCX_CUDA_TRY(cudaEventCreate(&e0));

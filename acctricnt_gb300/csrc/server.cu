@@ -69,7 +69,11 @@ extern "C" uint64_t accx_server_request_bytes(const accx_server *s, const accx_r
   // graph: offsets + entries; counting scratch: counts, owned-edge list,
   // per-vertex work and prefix arrays
   const uint64_t keys = 2 * draws;
-  return 3 * 8 * keys + 4ull * (n + 1) + 4 * keys + 4 * keys + 8 * (keys / 2) + 40ull * (n + 1);
+  uint64_t b = 3 * 8 * keys + 4ull * (n + 1) + 4 * keys + 4 * keys + 8 * (keys / 2) + 40ull * (n + 1);
+  // oriented counts: the relabeled copy (4(n+1) + 12m) and the oriented scratch
+  // (prefix lengths, reverse entries, partner ranges, work items)
+  if (s->cfg.count_orient) b += 4ull * (n + 1) + 12 * keys + 16 * keys + 12ull * (n + 1) + keys / 8;
+  return b;
 }
 
 static void run_request(accx_server *S, srv_req *q, accx_query_ctx *ctx, cudaStream_t st_query,
@@ -87,7 +91,11 @@ static void run_request(accx_server *S, srv_req *q, accx_query_ctx *ctx, cudaStr
   memset(&o, 0, sizeof(o));
   o.policy = S->cfg.count_policy;
   o.sm_limit = S->count_sms;
-  R.status = accx_cn_count(h, &o, nullptr, st);
+  if (S->cfg.count_orient) {
+    o.orient = 1;
+    R.status = accx_graph_relabel(h, st);  // prefix lists are short only on the degree-ordered copy
+  }
+  if (!R.status) R.status = accx_cn_count(h, &o, nullptr, st);
   if (!R.status) R.status = accx_cn_digest(h, &R.count_sum, &R.count_digest, st);
   R.n = h->n;
   R.m = h->m;

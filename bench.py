@@ -469,19 +469,19 @@ def run_batch(args):
     t0 = time.perf_counter()
     gs = [accx.Graph.generate(p) for p in params]
     gen_s = time.perf_counter() - t0
-    model, info = sched.default_model()
+    model, info = sched.default_model(orient=True)
     stream = torch.cuda.Stream()
     sp = stream.cuda_stream
     total_m = sum(G.m for G in gs)
     # one call sequence per graph (each graph relabeled and counted on its own)
     for G in gs:
         G.relabel(stream=sp)
-        G.set_model(model)
+        G.set_model(model, orient=True)
     torch.cuda.synchronize()
 
     def per_graph_step():
         for G in gs:
-            G.count(policy="model", out=None, stream=sp)
+            G.count(policy="model", out=None, stream=sp, orient=True)
             G.scan(0.3, 4, want_sim=False, want_label=False, want_cluster=False, stream=sp)
 
     for _ in range(args.warmup):
@@ -496,9 +496,9 @@ def run_batch(args):
     B = accx.Batch(gs)
     U = B.union
     U.relabel(stream=sp)
-    U.set_model(model)
-    kw, tune_ms, tune_all = U.autotune(policy="model", reps=2, stream=sp)
-    B.capture(policy="model", stream=sp, **kw)
+    U.set_model(model, orient=True)
+    kw, tune_ms, tune_all = U.autotune(policy="model", reps=2, stream=sp, orient=True)
+    B.capture(policy="model", stream=sp, orient=True, **kw)
     for _ in range(args.warmup):
         B.launch(stream=sp)
         U.scan(0.3, 4, want_sim=False, want_label=False, want_cluster=False, stream=sp)
@@ -543,9 +543,9 @@ def run_serve(args):
     gen_s = time.perf_counter() - t0
     t0 = time.perf_counter()
     G.relabel()
-    model, info = sched.default_model()
-    G.set_model(model)
-    G.count(policy="model", out=None)
+    model, info = sched.default_model(orient=True)
+    G.set_model(model, orient=True)
+    G.count(policy="model", out=None, orient=True)
     torch.cuda.synchronize()
     count_s = time.perf_counter() - t0
     rng = np.random.default_rng(7 + rank)
@@ -557,12 +557,12 @@ def run_serve(args):
             reqs.append(accx.query_request(float(rng.uniform(0.1, 0.9)), int(rng.integers(2, 21))))
     gaps = rng.exponential(1.0 / args.serve_rate, len(reqs))
     S = accx.Server(G, workers=args.serve_workers, hbm_budget=int(args.serve_budget_gb * (1 << 30)),
-                    count_policy="bitmap")
+                    count_policy="bitmap", count_orient=True)
     for r in reqs[:4]:  # warm each path once (contexts, per-graph arrays)
         S.wait(S.submit(r))
     S.close()
     S = accx.Server(G, workers=args.serve_workers, hbm_budget=int(args.serve_budget_gb * (1 << 30)),
-                    count_policy="bitmap")
+                    count_policy="bitmap", count_orient=True)
     ids = []
     t_start = time.perf_counter()
     t_next = t_start

@@ -401,6 +401,8 @@ typedef struct {
   uint64_t hbm_budget;        /* bytes requests may hold at once (0 = 64 GiB) */
   int count_policy;           /* policy for count requests (ACCX_POLICY_*, not TABLE) */
   int count_sm_percent;       /* SMs count requests may fill, percent (0 = 50); queries keep the rest */
+  int count_orient;           /* 1: count requests relabel their graph and count oriented
+                                 (accx_count_opts.orient; more HBM per request, less time) */
 } accx_server_config;
 typedef struct {
   uint64_t submitted, completed, failed;

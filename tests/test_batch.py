@@ -67,3 +67,24 @@ def test_autotuned_shape_counts_identically():
     kw, ms, allms = G.autotune(policy="bitmap", reps=1)
     assert ms > 0 and len(allms) >= 7
     assert np.array_equal(G.count(policy="bitmap", **kw), want)
+
+
+def test_oriented_capture_and_autotune_match_eager():
+    """Oriented counts in a captured batch replay and under the oriented
+    autotuner's launch shape equal the eager direct counts."""
+    import torch
+    gs, _ = _graphs()
+    B = accx.Batch(gs)
+    U = B.union
+    U.relabel()
+    want = U.count(policy="bitmap", bias=2)
+    s = torch.cuda.Stream()
+    kw, ms, allms = U.autotune(policy="bitmap", reps=1, stream=s.cuda_stream, orient=True)
+    assert ms > 0 and kw["window_kb"] in (32, 48, 64, 80, 96)
+    B.capture(policy="bitmap", bias=2, stream=s.cuda_stream, orient=True, **kw)
+    for _ in range(2):
+        U.count(policy="merge", bias=7, out=None)
+        torch.cuda.synchronize()
+        B.launch(stream=s.cuda_stream)
+        s.synchronize()
+        assert np.array_equal(U.read_counts(), want)

@@ -97,3 +97,24 @@ def test_admission_respects_the_hbm_budget():
     assert all(r.status == 0 for r in out)
     assert st["peak_bytes"] <= budget
     assert st["max_concurrent"] >= 2
+
+
+def test_oriented_count_requests_equal_direct_counts():
+    """count_orient: count requests relabel their graph and count oriented; the
+    digests equal those of the CPU oracle's counts, alone and in a mix."""
+    G = accx.Graph.generate(accx.rmat_params(12, 16, seed=5))
+    G.count(policy="heuristic", out=None)
+    reqs = [accx.count_request(accx.rmat_params(11 + i % 4, 16, seed=300 + i)) for i in range(8)]
+    plain = accx.Server(G, workers=1)
+    per_direct = plain.request_bytes(reqs[0])
+    plain.close()
+    S = accx.Server(G, workers=4, count_orient=True)
+    assert S.request_bytes(reqs[0]) > per_direct  # relabel + oriented scratch admitted
+    ids = [S.submit(r) for r in reqs]
+    out = [S.wait(i) for i in ids]
+    S.close()
+    for r, res in zip(reqs, out):
+        assert res.status == 0
+        o2, d2 = accx.generate_host(r.graph)
+        c2 = oracle.cn_count(o2, d2, nthreads=8) - 2
+        assert (res.count_sum, res.count_digest) == _count_digest(c2)

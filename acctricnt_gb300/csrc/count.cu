@@ -620,8 +620,9 @@ int accx_prefix_lengths(accx_graph *g, cudaStream_t s) {
 static int g_block_warps = 32;
 static int g_dense_kb = 128;
 static int g_sparse_kb = 64;
-static int g_or_dense_kb = 64;
-static int g_or_counter_kb = 16;
+static int g_or_dense_kb = 56;     // with 512-thread blocks two CTAs share an SM
+static int g_or_counter_kb = 8;
+static int g_or_block_warps = 16;
 
 
 static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s) {
@@ -629,7 +630,7 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s)
   int policy = o ? o->policy : ACCX_POLICY_HEURISTIC;
   int32_t bias = o ? o->bias : 0;
   const bool orient = o && o->orient;
-  int warps = (o && o->block_warps > 0) ? o->block_warps : g_block_warps;
+  int warps = (o && o->block_warps > 0) ? o->block_warps : (orient ? g_or_block_warps : g_block_warps);
   int dkb = (o && o->bitmap_window_kb > 0) ? o->bitmap_window_kb : (orient ? g_or_dense_kb : g_dense_kb);
   int skb = (o && o->sparse_table_kb > 0) ? o->sparse_table_kb : (orient ? g_or_counter_kb : g_sparse_kb);
   if (policy < ACCX_POLICY_HEURISTIC || policy > ACCX_POLICY_MODEL) return ACCX_ERR_INVALID_ARG;
@@ -717,12 +718,15 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s)
     k_gallop_or<<<sms * 8, MERGE_WARPS * 32, 0, s>>>(off, dst, g->d_pre, g->d_rev, g->d_edge_list, list_cap, ctr,
                                                      cnt);
     ACCX_MARK(3);
-    ACCX_CUDA_TRY(cudaFuncSetAttribute(k_bitmap_or, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // blocks of up to 512 threads use the half-size instance (two CTAs per SM when
+    // shared memory allows)
+    auto kb = warps <= 16 ? k_bitmap_or<512> : k_bitmap_or<1024>;
+    ACCX_CUDA_TRY(cudaFuncSetAttribute(kb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    ACCX_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bitmap_or, warps * 32, smem));
+    ACCX_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb, warps * 32, smem));
     if (per_sm < 1) return ACCX_ERR_INVALID_ARG;
-    k_bitmap_or<<<sms * per_sm, warps * 32, smem, s>>>(off, dst, g->d_pre, n, g->d_or_items, items_cap, work_u,
-                                                       g->d_prefix, g->d_or_sl, W, pcap, target, cnt, ctr);
+    kb<<<sms * per_sm, warps * 32, smem, s>>>(off, dst, g->d_pre, n, g->d_or_items, items_cap, work_u, g->d_prefix,
+                                              g->d_or_sl, W, pcap, target, cnt, ctr);
     ACCX_MARK(4);
     k_combine_or<<<tiles, 256, 0, s>>>(m, g->d_rev, cnt);
   } else {

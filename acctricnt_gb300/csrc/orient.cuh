@@ -167,7 +167,11 @@ __global__ void k_item_fill(const unsigned long long *__restrict__ icnt, const u
 // queue, so no warp waits behind one long list.  A hit at partner entry j
 // credits cnt[j] (RED), the owner's shared counter of the id's rank, and the
 // edge (shared per-entry counters, credited after the round).
-__global__ void __launch_bounds__(1024, 1) k_bitmap_or(const uint32_t *__restrict__ off,
+// NT = the block size the per-round arrays are sized for (blockDim.x <= NT); a
+// 512-thread instance needs half the static shared memory, so two CTAs fit an
+// SM when the window is small enough.
+template <int NT>
+__global__ void __launch_bounds__(NT, 1024 / NT) k_bitmap_or(const uint32_t *__restrict__ off,
                                                        const int32_t *__restrict__ dst,
                                                        const uint32_t *__restrict__ pre, uint32_t n,
                                                        const uint32_t *__restrict__ items, uint32_t items_cap,
@@ -184,8 +188,8 @@ __global__ void __launch_bounds__(1024, 1) k_bitmap_or(const uint32_t *__restric
   __shared__ unsigned long long s_it;
   __shared__ uint32_t s_tot, s_nseg, s_nlong, s_nlp, s_next;
   __shared__ uint32_t s_wsum[32], s_wcnt[32], s_wlong[32], s_wlp[32];
-  __shared__ uint32_t s_pre[1025], s_beg[1024], s_ent[1024], s_hit[1024];
-  __shared__ uint32_t s_lbeg[1024], s_llen[1024], s_lent[1024], s_lpc[1025], s_lhit[1024];
+  __shared__ uint32_t s_pre[NT + 1], s_beg[NT], s_ent[NT], s_hit[NT];
+  __shared__ uint32_t s_lbeg[NT], s_llen[NT], s_lent[NT], s_lpc[NT + 1], s_lhit[NT];
   const int tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
   for (uint32_t i = tid; i < nwords; i += nt) words[i] = 0;
@@ -318,7 +322,7 @@ __global__ void __launch_bounds__(1024, 1) k_bitmap_or(const uint32_t *__restric
 #pragma unroll
           for (int r = 0; r < PROBE_UNROLL; r++) {
             const uint32_t id = (uint32_t)xs[r];
-            if (xs[r] >= 0 && id < W) {
+            if (id < W) {  // also false for the -1 of lanes past the end
               const uint32_t wd = words[id >> 5], bit = 1u << (id & 31);
               if (wd & bit) {
                 const uint32_t rk = wbase[id >> 5] + __popc(wd & (bit - 1u));
@@ -354,7 +358,7 @@ __global__ void __launch_bounds__(1024, 1) k_bitmap_or(const uint32_t *__restric
 #pragma unroll
           for (int r = 0; r < LONG_UNROLL; r++) {
             const uint32_t id = (uint32_t)v[r];
-            if (v[r] >= 0 && id < W) {
+            if (id < W) {
               const uint32_t wd = words[id >> 5], bit = 1u << (id & 31);
               if (wd & bit) {
                 const uint32_t rk = wbase[id >> 5] + __popc(wd & (bit - 1u));

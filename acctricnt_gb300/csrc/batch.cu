@@ -86,8 +86,8 @@ extern "C" int accx_batch_create(accx_graph *const *graphs, int k, void *stream,
   accx_batch_desc *d_ds = nullptr;
   int rc = ACCX_OK;
   do {
-    if (cudaMalloc(&u->d_off, sizeof(uint32_t) * (N + 1)) != cudaSuccess ||
-        cudaMalloc(&u->d_dst, sizeof(int32_t) * (M + ACCX_DST_PAD)) != cudaSuccess ||
+    if (accx_dev_alloc((void **)&u->d_off, sizeof(uint32_t) * (N + 1), nullptr) != cudaSuccess ||
+        accx_dev_alloc((void **)&u->d_dst, sizeof(int32_t) * (M + ACCX_DST_PAD), nullptr) != cudaSuccess ||
         cudaMalloc(&d_ds, sizeof(accx_batch_desc) * k) != cudaSuccess) { rc = ACCX_ERR_OOM; break; }
     if (cudaMemcpyAsync(d_ds, ds.data(), sizeof(accx_batch_desc) * k, cudaMemcpyHostToDevice, s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
     uint32_t last = (uint32_t)M;

@@ -46,14 +46,47 @@ extern "C" const char *accx_strerror(int status) {
 
 extern "C" const char *accx_version(void) { return ACCX_VERSION_STR; }
 
-cudaError_t accx_dev_alloc(void **p, size_t bytes, cudaStream_t s) {
-  return s ? cudaMallocAsync(p, bytes, s) : cudaMalloc(p, bytes);
+// Device memory comes from the device's default stream-ordered pool, whose
+// release threshold is raised once per device so that freed blocks stay cached
+// for the next graph (creating and freeing graphs of the same size then costs no
+// page mapping).  cudaMemPoolTrimTo on cudaDeviceGetDefaultMemPool returns them.
+static void accx_pool_setup() {
+  static std::once_flag once[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    cudaGetLastError();
+    return;
+  }
+  std::call_once(once[dev], [dev] {
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t keep = UINT64_MAX;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    cudaGetLastError();
+  });
 }
 
+// With a stream: ordered on it.  Without: ordered on the legacy stream and
+// waited for, so the block is usable from any stream on return.
+cudaError_t accx_dev_alloc(void **p, size_t bytes, cudaStream_t s) {
+  accx_pool_setup();
+  if (s) return cudaMallocAsync(p, bytes, s);
+  cudaError_t e = cudaMallocAsync(p, bytes, 0);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+  return e;
+}
+
+// Without a stream the device is synchronised first, as cudaFree does: work on
+// any stream may still read the block.
 void accx_dev_free(void *p, cudaStream_t s) {
   if (!p) return;
-  if (s) cudaFreeAsync(p, s);
-  else cudaFree(p);
+  if (s) {
+    cudaFreeAsync(p, s);
+  } else {
+    cudaDeviceSynchronize();
+    cudaFreeAsync(p, 0);
+  }
 }
 
 bool accx_is_device_ptr(const void *p) {
@@ -66,17 +99,64 @@ bool accx_is_device_ptr(const void *p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// Host <-> device copies.  Pinned host memory is mapped into the GPU's address
+// space; on GB300 with its coherent host link a copy kernel moves it through
+// that mapping at link speed, where the copy engines were measured several
+// times slower into device blocks that had been freed and reused.  Pageable
+// host memory and unaligned ends go through cudaMemcpyAsync.
+__global__ void k_copy16(uint4 *__restrict__ d, const uint4 *__restrict__ s, size_t n16) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += (size_t)gridDim.x * blockDim.x)
+    d[i] = s[i];
+}
+
+// The device-side address of pinned (mapped) host memory, or nullptr.
+static void *mapped_host(const void *p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+static cudaError_t copy_via_kernel(void *d, const void *sp, size_t bytes, cudaStream_t s) {
+  const size_t n16 = bytes / 16, head = n16 * 16;
+  if (n16) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    k_copy16<<<accx_sm_count(dev) * 8, 256, 0, s>>>(static_cast<uint4 *>(d), static_cast<const uint4 *>(sp), n16);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  if (bytes > head)
+    return cudaMemcpyAsync(static_cast<char *>(d) + head, static_cast<const char *>(sp) + head, bytes - head,
+                           cudaMemcpyDefault, s);
+  return cudaSuccess;
+}
+
 int accx_copy_out(void *dst, const void *dev_src, size_t bytes, cudaStream_t s) {
   if (!bytes) return ACCX_OK;
-  ACCX_CUDA_TRY(cudaMemcpyAsync(dst, dev_src, bytes, cudaMemcpyDefault, s));
-  if (!accx_is_device_ptr(dst)) ACCX_CUDA_TRY(cudaStreamSynchronize(s));
+  if (accx_is_device_ptr(dst)) {
+    ACCX_CUDA_TRY(cudaMemcpyAsync(dst, dev_src, bytes, cudaMemcpyDefault, s));
+    return ACCX_OK;
+  }
+  void *m = mapped_host(dst);
+  if (m && !(((uintptr_t)m | (uintptr_t)dev_src) & 15)) ACCX_CUDA_TRY(copy_via_kernel(m, dev_src, bytes, s));
+  else ACCX_CUDA_TRY(cudaMemcpyAsync(dst, dev_src, bytes, cudaMemcpyDefault, s));
+  ACCX_CUDA_TRY(cudaStreamSynchronize(s));
   return ACCX_OK;
 }
 
 int accx_copy_in(void *dev_dst, const void *src, size_t bytes, cudaStream_t s) {
   if (!bytes) return ACCX_OK;
-  ACCX_CUDA_TRY(cudaMemcpyAsync(dev_dst, src, bytes, cudaMemcpyDefault, s));
-  if (!accx_is_device_ptr(src)) ACCX_CUDA_TRY(cudaStreamSynchronize(s));
+  if (accx_is_device_ptr(src)) {
+    ACCX_CUDA_TRY(cudaMemcpyAsync(dev_dst, src, bytes, cudaMemcpyDefault, s));
+    return ACCX_OK;
+  }
+  const void *m = mapped_host(src);
+  if (m && !(((uintptr_t)m | (uintptr_t)dev_dst) & 15)) ACCX_CUDA_TRY(copy_via_kernel(dev_dst, m, bytes, s));
+  else ACCX_CUDA_TRY(cudaMemcpyAsync(dev_dst, src, bytes, cudaMemcpyDefault, s));
+  ACCX_CUDA_TRY(cudaStreamSynchronize(s));
   return ACCX_OK;
 }
 
@@ -104,22 +184,45 @@ int accx_grid_for(int device, int block, int per_sm) {
 #define V_UNSORTED 4
 #define V_ASYM 8
 // Range checks always run (every kernel indexes off[] with neighbour ids); the
-// order, self-loop and symmetry checks run when `full` is set.
+// order, self-loop and symmetry checks run when `full` is set.  Symmetry: of the
+// two entries of a pair only the one whose target has the smaller degree (ties:
+// the larger target id) searches its reverse, in that shorter list, and the
+// searching entries are counted.  If every searching entry finds its reverse (a
+// non-searching entry; distinct entries have distinct reverses in sorted lists
+// without repeats) and they are exactly half of all entries, the reverse map is a
+// bijection onto the other half: the graph is symmetric.
 __global__ void k_validate(const uint32_t *__restrict__ off, const uint32_t *__restrict__ tilerow, const int32_t *__restrict__ dst, uint32_t n,
-                           uint32_t m, int full, int *__restrict__ status) {
+                           uint32_t m, int full, int *__restrict__ status, unsigned long long *__restrict__ searched) {
   __shared__ accx_tile_rows<256> sh;
   uint32_t base = blockIdx.x * 256u;
   uint32_t e = base + threadIdx.x;
   uint32_t u = accx_tile_row<256>(off, tilerow, n, m, base, e, &sh);
-  if (e >= m) return;
-  int32_t v = dst[e];
-  if (v < 0 || (uint32_t)v >= n) { atomicOr(status, V_RANGE); return; }
-  if (!full) return;
-  if ((uint32_t)v == u) { atomicOr(status, V_SELF); return; }
-  if (e > off[u] && dst[e - 1] >= v) { atomicOr(status, V_UNSORTED); return; }
-  uint32_t b = off[v], t = off[v + 1];
-  uint32_t r = accx_lower_bound(dst, b, t, (int32_t)u);
-  if (r >= t || dst[r] != (int32_t)u) atomicOr(status, V_ASYM);
+  int flag = 0;
+  bool chk = false;
+  if (e < m) {
+    const int32_t v = dst[e];
+    if (v < 0 || (uint32_t)v >= n) {
+      flag = V_RANGE;
+    } else if (full) {
+      if ((uint32_t)v == u) {
+        flag = V_SELF;
+      } else if (e > off[u] && dst[e - 1] >= v) {
+        flag = V_UNSORTED;
+      } else {
+        const uint32_t du = off[u + 1] - off[u], b = off[v], t = off[v + 1], dv = t - b;
+        chk = dv < du || (dv == du && (uint32_t)v > u);
+        if (chk) {
+          const uint32_t r = accx_lower_bound(dst, b, t, (int32_t)u);
+          if (r >= t || dst[r] != (int32_t)u) flag = V_ASYM;
+        }
+      }
+    }
+  }
+  if (flag) atomicOr(status, flag);
+  if (full) {  // uniform over the block
+    const int c = __syncthreads_count(chk);
+    if (threadIdx.x == 0 && c) atomicAdd(searched, (unsigned long long)c);
+  }
 }
 
 __global__ void k_tilerow(const uint32_t *__restrict__ off, uint32_t n, uint32_t m, uint32_t ntiles,
@@ -159,12 +262,12 @@ __global__ void k_check_offsets(const uint32_t *__restrict__ off, uint32_t n, ui
 }
 
 int accx_graph_validate_device(accx_graph *g, int full, cudaStream_t s) {
-  int *d_status = nullptr;
-  ACCX_CUDA_TRY(cudaMalloc(&d_status, sizeof(int)));
-  int zero = 0;
+  int *d_status = nullptr;  // [0] defect bits, [2..3] searched-entry count (8-byte aligned)
+  ACCX_CUDA_TRY(cudaMalloc(&d_status, 4 * sizeof(int)));
+  unsigned long long *d_searched = reinterpret_cast<unsigned long long *>(d_status + 2);
   int rc = ACCX_OK;
   do {
-    if (cudaMemcpyAsync(d_status, &zero, sizeof(int), cudaMemcpyHostToDevice, s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
+    if (cudaMemsetAsync(d_status, 0, 4 * sizeof(int), s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
     k_check_offsets<<<accx_grid_for(g->device, 256, 4), 256, 0, s>>>(g->d_off, g->n, (uint32_t)g->m, d_status);
     int st = 0;
     if (cudaMemcpyAsync(&st, d_status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
@@ -173,9 +276,13 @@ int accx_graph_validate_device(accx_graph *g, int full, cudaStream_t s) {
     if ((rc = accx_tilerow_build(g, g->d_off, &g->d_tilerow, s)) != ACCX_OK) break;
     if (g->m) {
       uint32_t blocks = (uint32_t)((g->m + 255) / 256);
-      k_validate<<<blocks, 256, 0, s>>>(g->d_off, g->d_tilerow, g->d_dst, g->n, (uint32_t)g->m, full, d_status);
+      k_validate<<<blocks, 256, 0, s>>>(g->d_off, g->d_tilerow, g->d_dst, g->n, (uint32_t)g->m, full, d_status,
+                                        d_searched);
+      unsigned long long searched = 0;
       if (cudaMemcpyAsync(&st, d_status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+          cudaMemcpyAsync(&searched, d_searched, sizeof(searched), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
           cudaStreamSynchronize(s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
+      if (full && !st && 2 * searched != g->m) st = V_ASYM;
       rc = (st & V_RANGE) ? ACCX_ERR_RANGE : (st & V_SELF) ? ACCX_ERR_SELF_LOOP
          : (st & V_UNSORTED) ? ACCX_ERR_UNSORTED : (st & V_ASYM) ? ACCX_ERR_ASYMMETRIC : ACCX_OK;
     }
@@ -199,8 +306,8 @@ static int alloc_graph(uint32_t n, uint64_t m, accx_graph **out) {
   g->device = dev;
   g->n = n;
   g->m = m;
-  if (cudaMalloc(&g->d_off, sizeof(uint32_t) * ((size_t)n + 1)) != cudaSuccess ||
-      cudaMalloc(&g->d_dst, sizeof(int32_t) * ((size_t)m + ACCX_DST_PAD)) != cudaSuccess) {
+  if (accx_dev_alloc((void **)&g->d_off, sizeof(uint32_t) * ((size_t)n + 1), nullptr) != cudaSuccess ||
+      accx_dev_alloc((void **)&g->d_dst, sizeof(int32_t) * ((size_t)m + ACCX_DST_PAD), nullptr) != cudaSuccess) {
     cudaGetLastError();
     accx_graph_free(g);
     return ACCX_ERR_OOM;

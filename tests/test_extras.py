@@ -59,3 +59,28 @@ def test_vertex_ranges_equal_the_reference_partitioner(parts):
     G = accx.Graph.generate(accx.rmat_params(16, 16, seed=5))
     off, dst = G.download()
     assert np.array_equal(G.vertex_ranges(parts), oracle.vertex_ranges(off, dst, parts))
+
+
+@pytest.mark.gpu
+def test_pinned_host_buffers_roundtrip():
+    """Graph upload and count download through pinned (GPU-mapped) host buffers
+    -- the copy-kernel path -- equal the pageable path, for sizes that are not
+    multiples of 16 bytes and for a buffer that starts 4 bytes into its block."""
+    import ctypes
+    import torch
+    off, dst = accx.generate_host(accx.rmat_params(13, 7, seed=21))
+    n, m = len(off) - 1, len(dst)
+    ref = accx.Graph.from_csr(off, dst).count(policy="bitmap", bias=2)
+    for shift in (0, 1):
+        t_off = torch.zeros(n + 1 + shift, dtype=torch.int32).pin_memory()
+        t_dst = torch.zeros(m + shift, dtype=torch.int32).pin_memory()
+        t_off[shift:] = torch.from_numpy(off.view(np.int32))
+        t_dst[shift:] = torch.from_numpy(dst)
+        H = accx.Graph.from_device(t_off.data_ptr() + 4 * shift, t_dst.data_ptr() + 4 * shift, n, m, validate=True)
+        o2, d2 = H.download()
+        assert np.array_equal(o2, off) and np.array_equal(d2, dst)
+        out = torch.full((m + shift,), -7, dtype=torch.int32).pin_memory()
+        H.count(policy="bitmap", bias=2, orient=True, out=None)
+        accx._check(accx.lib.accx_cn_read(H._h, ctypes.c_void_p(out.data_ptr() + 4 * shift), None), "cn_read")
+        assert np.array_equal(out[shift:].numpy(), ref)
+        H.free()

@@ -35,14 +35,17 @@ struct accx_tile_rows {
   uint32_t r_lo, r_hi;
 };
 
+// The same for tile `tile` (base = tile * TILE), for CTAs that loop over tiles;
+// such a loop must put a __syncthreads between two calls (sh is rewritten).
 template <int TILE>
-__device__ __forceinline__ uint32_t accx_tile_row(const uint32_t *__restrict__ off,
-                                                  const uint32_t *__restrict__ tilerow, uint32_t n, uint32_t m,
-                                                  uint32_t base, uint32_t e, accx_tile_rows<TILE> *sh) {
+__device__ __forceinline__ uint32_t accx_tile_row_at(const uint32_t *__restrict__ off,
+                                                     const uint32_t *__restrict__ tilerow, uint32_t n, uint32_t m,
+                                                     uint32_t tile, uint32_t base, uint32_t e,
+                                                     accx_tile_rows<TILE> *sh) {
   if (tilerow) {
     if (threadIdx.x == 0) {
-      sh->r_lo = __ldg(tilerow + blockIdx.x);
-      sh->r_hi = __ldg(tilerow + blockIdx.x + 1);
+      sh->r_lo = __ldg(tilerow + tile);
+      sh->r_hi = __ldg(tilerow + tile + 1);
     }
   } else {
     if (threadIdx.x == 0) sh->r_lo = accx_row_of(off, 0, n, base);
@@ -56,6 +59,13 @@ __device__ __forceinline__ uint32_t accx_tile_row(const uint32_t *__restrict__ o
   uint32_t r = 0;
   if (e < m) r = accx_row_of(off, sh->r_lo, sh->r_hi + 1, e);
   return r;
+}
+
+template <int TILE>
+__device__ __forceinline__ uint32_t accx_tile_row(const uint32_t *__restrict__ off,
+                                                  const uint32_t *__restrict__ tilerow, uint32_t n, uint32_t m,
+                                                  uint32_t base, uint32_t e, accx_tile_rows<TILE> *sh) {
+  return accx_tile_row_at<TILE>(off, tilerow, n, m, blockIdx.x, base, e, sh);
 }
 
 // Degree-owner rule of the reference CPU bitmap build (scan-query/scan_xp.cpp:290-292):

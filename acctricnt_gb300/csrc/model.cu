@@ -208,12 +208,17 @@ __global__ void __launch_bounds__(TILE) k_bucket_stats(const uint32_t *__restric
   __shared__ accx_tile_rows<TILE> sh;
   __shared__ unsigned long long hs[3 * NBB];
   for (int i = threadIdx.x; i < 3 * NBB; i += TILE) hs[i] = 0;
-  uint32_t base = blockIdx.x * (uint32_t)TILE;
+  // many tiles per CTA: the shared histograms reach the device counters once per CTA
+  const uint32_t ntiles = (m + TILE - 1) / TILE;
+  for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  __syncthreads();
+  uint32_t base = tile * (uint32_t)TILE;
   uint32_t e = base + threadIdx.x;
-  uint32_t u = accx_tile_row<TILE>(off, tilerow, n, m, base, e, &sh);  // contains __syncthreads
+  uint32_t u = accx_tile_row_at<TILE>(off, tilerow, n, m, tile, base, e, &sh);  // contains __syncthreads
+  int b = -1;
+  uint32_t du = 0, dv = 0;
   if (e < m) {
     uint32_t v = (uint32_t)dst[e];
-    uint32_t du, dv;
     if (ORIENT) {
       du = pre[u];
       dv = pre[v];
@@ -221,12 +226,22 @@ __global__ void __launch_bounds__(TILE) k_bucket_stats(const uint32_t *__restric
       du = off[u + 1] - off[u];
       dv = off[v + 1] - off[v];
     }
-    if ((!ORIENT || dv > 0) && accx_owns(u, du, v, dv)) {
-      int b = accx_bucket(du) * ACCX_NB + accx_bucket(dv);
-      atomicAdd(&hs[b], 1ull);
-      atomicAdd(&hs[NBB + b], (unsigned long long)du);
-      atomicAdd(&hs[2 * NBB + b], (unsigned long long)dv);
+    if ((!ORIENT || dv > 0) && accx_owns(u, du, v, dv)) b = accx_bucket(du) * ACCX_NB + accx_bucket(dv);
+  }
+  // lanes of one bucket add up first (most of a warp lands in a few buckets);
+  // sizes are summed as 16-bit halves, so 32 lanes cannot overflow 32 bits
+  const unsigned peers = __match_any_sync(ACCX_FULL_MASK, b);
+  if (b >= 0) {
+    const unsigned long long su = ((unsigned long long)__reduce_add_sync(peers, du >> 16) << 16) +
+                                  __reduce_add_sync(peers, du & 0xffffu);
+    const unsigned long long sv = ((unsigned long long)__reduce_add_sync(peers, dv >> 16) << 16) +
+                                  __reduce_add_sync(peers, dv & 0xffffu);
+    if ((threadIdx.x & 31) == __ffs(peers) - 1) {
+      atomicAdd(&hs[b], (unsigned long long)__popc(peers));
+      atomicAdd(&hs[NBB + b], su);
+      atomicAdd(&hs[2 * NBB + b], sv);
     }
+  }
   }
   __syncthreads();
   for (int i = threadIdx.x; i < 3 * NBB; i += TILE)
@@ -295,12 +310,12 @@ static int ensure_features(accx_graph *g, cudaStream_t s, int mode) {
   ACCX_CUDA_TRY(cudaMemsetAsync(st->d_stats[mode], 0, sizeof(unsigned long long) * 3 * NBB, s));
   const uint32_t m = (uint32_t)g->m;
   if (mode == 0) {
-    if (m) k_bucket_stats<256, false><<<(m + 255) / 256, 256, 0, s>>>(g->d_off, g->d_tilerow, g->d_dst, g->n, m,
+    if (m) k_bucket_stats<256, false><<<min((m + 255) / 256, (uint32_t)accx_sm_count(g->device) * 8), 256, 0, s>>>(g->d_off, g->d_tilerow, g->d_dst, g->n, m,
                                                                     st->d_stats[0], nullptr);
   } else if (m) {
     int rc = accx_prefix_lengths(g, s);
     if (rc) return rc;
-    k_bucket_stats<256, true><<<(m + 255) / 256, 256, 0, s>>>(off, rel ? g->d_rtilerow : g->d_tilerow,
+    k_bucket_stats<256, true><<<min((m + 255) / 256, (uint32_t)accx_sm_count(g->device) * 8), 256, 0, s>>>(off, rel ? g->d_rtilerow : g->d_tilerow,
                                                              rel ? g->d_rdst : g->d_dst, g->n, m, st->d_stats[1],
                                                              g->d_pre);
   }

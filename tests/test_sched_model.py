@@ -71,8 +71,15 @@ def test_learned_schedule_beats_the_reference_heuristic_on_an_unseen_graph():
     G.relabel()
     edges, T = sched.bucket_timings(G, reps=2)
     e, so, sp = G.bucket_stats()
-    t_model = sched.table_time(model.table_for(G), T)
-    t_heur = sched.table_time(sched.heuristic_table(e, so, sp), T)
-    r = sched.regret(model.table_for(G), edges, T)
+    heur = sched.heuristic_table(e, so, sp)
+    # the network's own choice (no kind offset) against buckets timed alone
+    bias = model.kind_bias()
+    model.set_kind_bias([0.0, 0.0, 0.0])
+    raw = model.table_for(G)
+    assert sched.table_time(raw, T) < sched.table_time(heur, T)
+    assert sched.regret(raw, edges, T)["regret_frac"] < 0.5
+    # with the offset fitted on whole counts: faster than the rule as a whole count
+    model.set_kind_bias(bias)
+    t_model = sched._count_phase_ms(G, model.table_for(G).reshape(-1), 3)
+    t_heur = sched._count_phase_ms(G, heur.reshape(-1), 3)
     assert t_model < t_heur
-    assert r["regret_frac"] < 0.5

@@ -73,6 +73,7 @@ struct accx_graph {
   uint2 *d_or_sl = nullptr;                // m oriented bitmap entries: (partner prefix start, cut length), 0 length = not bitmap
   uint32_t *d_or_items = nullptr;          // n + m/32 + 1 oriented bitmap work items: owner of each
   uint32_t *d_rev = nullptr;               // m reverse entry of every entry of the counting CSR (oriented counts)
+  uint32_t *d_rev_orig = nullptr;          // m reverse entries of the handle's own CSR, recorded by full validation
   const uint32_t *rev_csr = nullptr;       // the offsets array d_rev was built for
   void *d_scan_tmp = nullptr;
   size_t scan_tmp_bytes = 0;

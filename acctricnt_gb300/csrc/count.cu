@@ -701,8 +701,14 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s)
     // reverse entries: built on the first oriented count of this CSR and kept
     // (an index of the graph, like the tile rows)
     if (g->rev_csr != off) {
-      ACCX_CUDA_TRY(cudaMemsetAsync(g->d_rev, 0xff, sizeof(uint32_t) * (size_t)m, s));
-      k_rev_build<256><<<tiles, 256, 0, s>>>(off, tilerow, dst, g->d_pre, n, m, g->d_rev);
+      if (g->d_rev_orig && !rel) {  // recorded by validation for this very CSR
+        ACCX_CUDA_TRY(cudaMemcpyAsync(g->d_rev, g->d_rev_orig, sizeof(uint32_t) * (size_t)m, cudaMemcpyDeviceToDevice, s));
+      } else if (g->d_rev_orig) {
+        k_rev_compose<<<sms * 8, 256, 0, s>>>(g->d_rmap, g->d_rev_orig, m, g->d_rev);
+      } else {
+        ACCX_CUDA_TRY(cudaMemsetAsync(g->d_rev, 0xff, sizeof(uint32_t) * (size_t)m, s));
+        k_rev_build<256><<<tiles, 256, 0, s>>>(off, tilerow, dst, g->d_pre, n, m, g->d_rev);
+      }
       g->rev_csr = off;
     }
     k_classify<256, true><<<tiles, 256, 0, s>>>(off, tilerow, dst, n, m, policy, g->d_table, g->d_edge_list, list_cap,

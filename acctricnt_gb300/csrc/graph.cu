@@ -192,7 +192,8 @@ int accx_grid_for(int device, int block, int per_sm) {
 // without repeats) and they are exactly half of all entries, the reverse map is a
 // bijection onto the other half: the graph is symmetric.
 __global__ void k_validate(const uint32_t *__restrict__ off, const uint32_t *__restrict__ tilerow, const int32_t *__restrict__ dst, uint32_t n,
-                           uint32_t m, int full, int *__restrict__ status, unsigned long long *__restrict__ searched) {
+                           uint32_t m, int full, int *__restrict__ status, unsigned long long *__restrict__ searched,
+                           uint32_t *__restrict__ rev) {
   __shared__ accx_tile_rows<256> sh;
   uint32_t base = blockIdx.x * 256u;
   uint32_t e = base + threadIdx.x;
@@ -213,7 +214,12 @@ __global__ void k_validate(const uint32_t *__restrict__ off, const uint32_t *__r
         chk = dv < du || (dv == du && (uint32_t)v > u);
         if (chk) {
           const uint32_t r = accx_lower_bound(dst, b, t, (int32_t)u);
-          if (r >= t || dst[r] != (int32_t)u) flag = V_ASYM;
+          if (r >= t || dst[r] != (int32_t)u) {
+            flag = V_ASYM;
+          } else if (rev) {  // a valid graph's pairs cover every entry: the reverse index for free
+            rev[e] = r;
+            rev[r] = e;
+          }
         }
       }
     }
@@ -276,8 +282,13 @@ int accx_graph_validate_device(accx_graph *g, int full, cudaStream_t s) {
     if ((rc = accx_tilerow_build(g, g->d_off, &g->d_tilerow, s)) != ACCX_OK) break;
     if (g->m) {
       uint32_t blocks = (uint32_t)((g->m + 255) / 256);
+      uint32_t *rev = nullptr;
+      if (full && !g->d_rev_orig && accx_dev_alloc((void **)&rev, sizeof(uint32_t) * (size_t)g->m, nullptr) != cudaSuccess) {
+        cudaGetLastError();
+        rev = nullptr;  // no room: counts build the index themselves
+      }
       k_validate<<<blocks, 256, 0, s>>>(g->d_off, g->d_tilerow, g->d_dst, g->n, (uint32_t)g->m, full, d_status,
-                                        d_searched);
+                                        d_searched, rev);
       unsigned long long searched = 0;
       if (cudaMemcpyAsync(&st, d_status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
           cudaMemcpyAsync(&searched, d_searched, sizeof(searched), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
@@ -285,6 +296,10 @@ int accx_graph_validate_device(accx_graph *g, int full, cudaStream_t s) {
       if (full && !st && 2 * searched != g->m) st = V_ASYM;
       rc = (st & V_RANGE) ? ACCX_ERR_RANGE : (st & V_SELF) ? ACCX_ERR_SELF_LOOP
          : (st & V_UNSORTED) ? ACCX_ERR_UNSORTED : (st & V_ASYM) ? ACCX_ERR_ASYMMETRIC : ACCX_OK;
+      if (rev) {
+        if (rc == ACCX_OK) g->d_rev_orig = rev;  // complete only for a graph that passed
+        else accx_dev_free(rev, nullptr);
+      }
     }
   } while (0);
   cudaFree(d_status);
@@ -392,7 +407,7 @@ extern "C" int accx_graph_free(accx_graph *g) {
   if (!g) return ACCX_ERR_INVALID_ARG;
   void *ptrs[] = {g->d_off,      g->d_dst,    g->d_cnt,  g->d_edge_list, g->d_icnt,  g->d_prefix, g->d_scan_tmp,
                   g->d_counters, g->d_table,  g->d_roff, g->d_rdst,      g->d_rmap,  g->d_rcnt,   g->d_oldid,
-                  g->d_newid,    g->d_simkey, g->d_tilerow, g->d_rtilerow, g->d_src, g->d_pre, g->d_or_sl, g->d_or_items, g->d_rev};
+                  g->d_newid,    g->d_simkey, g->d_tilerow, g->d_rtilerow, g->d_src, g->d_pre, g->d_or_sl, g->d_or_items, g->d_rev, g->d_rev_orig};
   accx_query_ctx_release(&g->qc);
   for (void *p : ptrs) accx_dev_free(p, g->home);
   for (int i = 0; i <= ACCX_NUM_PHASES; i++)

@@ -416,7 +416,10 @@ def run_gb300(args):
             "phases_ms": {k: round(v, 3) for k, v in phases.items()}, "kinds": stats,
             "matches": ({"found": matches[0], "bitmap_probed": matches[1]} if matches else None),
             "scan": scan, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-            "gpu_launches": ((8 if policy == "model" else 7) + (1 if orient else 0)) * args.steps,
+            # this library's kernels per count: model inference (model policy); direct: classify, item
+            # counts, merge, gallop, bitmap, mirror; oriented: fill, prefix lengths, classify, item
+            # counts, item fill, merge, gallop, bitmap, combine; gather back (relabeled graph)
+            "gpu_launches": ((1 if policy == "model" else 0) + (9 if orient else 6) + 1) * args.steps,
             "clocks": clk.summary(),
             "sched": sched_info}
     if rank == 0:

@@ -238,7 +238,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bitmap_or(const uint32_t *__r
       probed += len;
       const bool is_short = len > 0 && len < LONG_SEG, is_long = len >= LONG_SEG;
       const unsigned bs = __ballot_sync(ACCX_FULL_MASK, is_short), bl = __ballot_sync(ACCX_FULL_MASK, is_long);
-      const uint32_t lp = is_long ? (len + LONG_PIECE - 1) / LONG_PIECE : 0u;
+      // long lists are cut into pieces on even entry boundaries (8-byte loads)
+      const uint32_t lp = is_long ? (len + (sst & 1u) + LONG_PIECE - 1) / LONG_PIECE : 0u;
       uint32_t incl = is_short ? len : 0u, lincl = lp;
 #pragma unroll
       for (int d = 1; d < 32; d <<= 1) {
@@ -354,24 +355,29 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bitmap_or(const uint32_t *__r
             hi = nh < hi ? nh : hi;
           }
           const uint32_t q = lo;
-          const uint32_t a1 = s_lbeg[q] + s_llen[q];
-          const uint32_t j0 = s_lbeg[q] + (pl - s_lpc[q]) * LONG_PIECE;
-          int32_t v[LONG_UNROLL];
+          const uint32_t a0 = s_lbeg[q], a1 = a0 + s_llen[q];
+          // the piece spans [j0, j0 + LONG_PIECE) from the even entry at or before the
+          // list start; lane pairs (j, j+1) come from one 8-byte load, ids outside
+          // [a0, a1) are dropped (the array's padding keeps the last pair in bounds)
+          const uint32_t j0 = (a0 & ~1u) + (pl - s_lpc[q]) * LONG_PIECE;
+          int2 v[LONG_UNROLL / 2];
 #pragma unroll
-          for (int r = 0; r < LONG_UNROLL; r++) {
-            const uint32_t j = j0 + 32u * r + (uint32_t)lane;
-            v[r] = j < a1 ? __ldg(dst + j) : -1;
+          for (int r = 0; r < LONG_UNROLL / 2; r++) {
+            const uint32_t j = j0 + 64u * r + 2u * (uint32_t)lane;
+            v[r] = j < a1 ? __ldg(reinterpret_cast<const int2 *>(dst + j)) : make_int2(-1, -1);
+            if (j < a0) v[r].x = -1;
+            if (j + 1u >= a1) v[r].y = -1;
           }
           uint32_t h = 0;
 #pragma unroll
           for (int r = 0; r < LONG_UNROLL; r++) {
-            const uint32_t id = (uint32_t)v[r];
+            const uint32_t id = (uint32_t)((r & 1) ? v[r >> 1].y : v[r >> 1].x);
             if (id < W) {
               const uint32_t wd = words[id >> 5], bit = 1u << (id & 31);
               if (wd & bit) {
                 const uint32_t rk = wbase[id >> 5] + __popc(wd & (bit - 1u));
                 h++;
-                atomicAdd(cnt + j0 + 32u * r + (uint32_t)lane, 1);
+                atomicAdd(cnt + j0 + 64u * (r >> 1) + 2u * (uint32_t)lane + (uint32_t)(r & 1), 1);
                 if (rk < pxs) atomicAdd(&ocnt[rk], 1u);
               }
             }

@@ -18,7 +18,8 @@ HOST = os.path.join(PKG, "host")
 BUILD = os.path.join(PKG, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 LIB = os.path.join(BUILD, "libaccx.so")
-CLIS = {"scan-xp-gb300": "main_scanxp.cpp", "scan-xp-gb300-varying": "main_scanxp_varying.cpp"}
+CLIS = {"scan-xp-gb300": "main_scanxp.cpp", "scan-xp-gb300-varying": "main_scanxp_varying.cpp",
+        "edge-list-to-bins-gb300": "main_edgelist.cpp"}
 CLI = os.path.join(BUILD, "scan-xp-gb300")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -10,7 +10,8 @@ host generators); run from the repository root:
 Each fixture <name>.npz holds the graph (off, dst), the query (eps, mu) and the
 reference's outputs: cnn (= 2 + common-neighbour count per CSR entry), sim,
 label (final, 0/1/2), cluster (min-id cluster of cores, -1 otherwise) and the
-bytes of its scanxp-result-<eps>-<mu>.txt file.
+bytes of its scanxp-result-<eps>-<mu>.txt file.  edge_list_converter.npz holds a
+text edge list and the two files the reference's converter writes for it.
 """
 import os
 import sys
@@ -76,6 +77,45 @@ def seeded_graphs():
     return g
 
 
+def edge_list_text():
+    """A text edge list with comments, self loops, reversed copies of edges
+    (dropped by the converter), isolated ids below the largest one and tab
+    separators; no repeated (i < j) pair and no blank line (the reference reads
+    uninitialised ids for a line without two numbers)."""
+    rng = np.random.default_rng(11)
+    lines = ["# Directed graph (each unordered pair on one line)", "# FromNodeId\tToNodeId"]
+    pairs = set()
+    while len(pairs) < 400:
+        a, b = (int(x) for x in rng.integers(0, 180, 2))
+        if a != b:
+            pairs.add((min(a, b), max(a, b)))
+    for a, b in sorted(pairs, key=lambda p: (p[1] * 7 + p[0]) % 97):
+        lines.append("%d\t%d" % (a, b))
+        if (a + b) % 5 == 0:
+            lines.append("%d %d" % (b, a))  # reversed copy
+    lines += ["7 7", "199 250", "# trailing comment", "3 260"]
+    return ("\n".join(lines) + "\n").encode()
+
+
+def edge_list_fixture():
+    """Runs the reference converter (oracle/_ref/edge-list-converter) on the text."""
+    import subprocess
+    d = tempfile.mkdtemp(prefix="golden_el_")
+    src = os.path.join(d, "edges.txt")
+    with open(src, "wb") as f:
+        f.write(edge_list_text())
+    exe = os.path.join(ROOT, "oracle", "_ref", "edge-list-converter")
+    subprocess.run([exe, src, os.path.join(d, "b_degree.bin"), os.path.join(d, "b_adj.bin")], check=True,
+                   capture_output=True)
+    out = {}
+    for k in ("edges.txt", "b_degree.bin", "b_adj.bin"):
+        with open(os.path.join(d, k), "rb") as f:
+            out[k.replace(".", "_")] = np.frombuffer(f.read(), np.uint8)
+    np.savez_compressed(os.path.join(HERE, "edge_list_converter.npz"), **out)
+    print("edge_list_converter      text=%d bytes degree=%d bytes adj=%d bytes" % (
+        len(out["edges_txt"]), len(out["b_degree_bin"]), len(out["b_adj_bin"])))
+
+
 def main():
     oracle.build()
     if not oracle.have_reference():
@@ -96,6 +136,7 @@ def main():
         print("%-24s n=%-6d m=%-7d cores=%-5d hubs=%-4d pairs-lines=%d" % (
             name, len(off) - 1, len(dst), int((ref["label"] == 1).sum()), int((ref["label"] == 2).sum()),
             result.count(b"\nn ")))
+    edge_list_fixture()
 
 
 if __name__ == "__main__":

@@ -190,8 +190,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bitmap_or(const uint32_t *__r
                                                        unsigned long long *__restrict__ ctr) {
   extern __shared__ __align__(16) uint32_t smem[];
   const uint32_t nwords = W / 32;
-  uint32_t *words = smem;                                          // nwords
-  uint32_t *ocnt = smem + nwords;                                  // pcap owner-prefix counters
+  uint32_t *words = smem;                                          // nwords + a zero word (ids >= W probe it)
+  uint32_t *ocnt = smem + nwords + 4;                              // pcap owner-prefix counters
   uint16_t *wbase = reinterpret_cast<uint16_t *>(ocnt + pcap);     // nwords first-id positions
   __shared__ unsigned long long s_it;
   __shared__ uint32_t s_tot, s_nseg, s_nlong, s_nlp, s_next;
@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bitmap_or(const uint32_t *__r
   __shared__ uint32_t s_lbeg[NT], s_llen[NT], s_lent[NT], s_lpc[NT + 1], s_lhit[NT];
   const int tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
-  for (uint32_t i = tid; i < nwords; i += nt) words[i] = 0;
+  for (uint32_t i = tid; i <= nwords; i += nt) words[i] = 0;
   unsigned long long total = prefix[n];
   if (total > items_cap) total = items_cap;
   unsigned long long found = 0, probed = 0;  // this thread's share, summed per warp at the end
@@ -330,15 +330,14 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bitmap_or(const uint32_t *__r
           }
 #pragma unroll
           for (int r = 0; r < PROBE_UNROLL; r++) {
-            const uint32_t id = (uint32_t)xs[r];
-            if (id < W) {  // also false for the -1 of lanes past the end
-              const uint32_t wd = words[id >> 5], bit = 1u << (id & 31);
-              if (wd & bit) {
-                const uint32_t rk = wbase[id >> 5] + __popc(wd & (bit - 1u));
-                atomicAdd(cnt + gi[r], 1);
-                if (rk < pxs) atomicAdd(&ocnt[rk], 1u);  // always true on a sorted CSR
-                atomicAdd(&s_hit[sg[r]], 1u);
-              }
+            // ids >= W (the -1 of lanes past the end) read the zero word
+            const uint32_t id = min((uint32_t)xs[r], W);
+            const uint32_t wd = words[id >> 5];
+            if ((wd >> (id & 31u)) & 1u) {
+              const uint32_t rk = wbase[id >> 5] + __popc(wd & ((1u << (id & 31u)) - 1u));
+              atomicAdd(cnt + gi[r], 1);
+              if (rk < pxs) atomicAdd(&ocnt[rk], 1u);  // always true on a sorted CSR
+              atomicAdd(&s_hit[sg[r]], 1u);
             }
           }
         } else {
@@ -368,18 +367,21 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bitmap_or(const uint32_t *__r
             if (j < a0) v[r].x = -1;
             if (j + 1u >= a1) v[r].y = -1;
           }
+          // the warp stops at the first pair group past the list end (the last
+          // piece of a list is mostly shorter than LONG_PIECE)
+          const uint32_t rem = a1 - j0;
+          int32_t *const cl = cnt + j0 + 2u * (uint32_t)lane;
           uint32_t h = 0;
 #pragma unroll
           for (int r = 0; r < LONG_UNROLL; r++) {
-            const uint32_t id = (uint32_t)((r & 1) ? v[r >> 1].y : v[r >> 1].x);
-            if (id < W) {
-              const uint32_t wd = words[id >> 5], bit = 1u << (id & 31);
-              if (wd & bit) {
-                const uint32_t rk = wbase[id >> 5] + __popc(wd & (bit - 1u));
-                h++;
-                atomicAdd(cnt + j0 + 64u * (r >> 1) + 2u * (uint32_t)lane + (uint32_t)(r & 1), 1);
-                if (rk < pxs) atomicAdd(&ocnt[rk], 1u);
-              }
+            if (64u * (uint32_t)(r >> 1) >= rem) break;
+            const uint32_t id = min((uint32_t)((r & 1) ? v[r >> 1].y : v[r >> 1].x), W);
+            const uint32_t wd = words[id >> 5];
+            if ((wd >> (id & 31u)) & 1u) {
+              const uint32_t rk = wbase[id >> 5] + __popc(wd & ((1u << (id & 31u)) - 1u));
+              h++;
+              atomicAdd(cl + 64u * (r >> 1) + (uint32_t)(r & 1), 1);
+              if (rk < pxs) atomicAdd(&ocnt[rk], 1u);
             }
           }
           h = __reduce_add_sync(ACCX_FULL_MASK, h);

@@ -106,6 +106,7 @@ def _load():
         "accx_graph_generate": (C.c_int, [C.POINTER(GenParams), P, C.POINTER(P)]),
         "accx_graph_relabel": (C.c_int, [P, P]),
         "accx_graph_is_relabeled": (C.c_int, [P]),
+        "accx_graph_relabeled_csr": (C.c_int, [P, P, P, P, P, P]),
         "accx_generate_host": (C.c_int, [C.POINTER(GenParams), C.POINTER(C.c_uint32), C.POINTER(C.c_uint64), P, P]),
         "accx_write_graph_dir": (C.c_int, [C.c_char_p, P, P, C.c_uint32, C.c_uint64]),
         "accx_cn_count": (C.c_int, [P, C.POINTER(CountOpts), P, P]),
@@ -319,6 +320,18 @@ class Graph:
     @property
     def relabeled(self):
         return bool(lib.accx_graph_is_relabeled(self._h))
+
+    def relabeled_csr(self):
+        """(roff, rdst, map, oldid) of the relabeled copy: map[e] = the relabeled
+        position of original entry e, oldid[new id] = original id."""
+        n, m = self.n, self.m
+        roff = np.zeros(n + 1, np.uint32)
+        rdst = np.zeros(max(m, 1), np.int32)
+        rmap = np.zeros(max(m, 1), np.uint32)
+        oldid = np.zeros(max(n, 1), np.uint32)
+        _check(lib.accx_graph_relabeled_csr(self._h, _ptr(roff), _ptr(rdst), _ptr(rmap), _ptr(oldid), None),
+               "graph_relabeled_csr")
+        return roff, rdst[:m], rmap[:m], oldid[:n]
 
     def free(self):
         if self._h and not getattr(self, "_owned_by_batch", False):

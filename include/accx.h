@@ -83,6 +83,14 @@ int accx_graph_size(const accx_graph *g, uint32_t *n, uint64_t *m);
 int accx_graph_relabel(accx_graph *g, void *stream);
 int accx_graph_is_relabeled(const accx_graph *g);
 
+/* Copies the relabeled CSR and its maps out (host or device pointers; any may
+ * be NULL): roff[n+1], rdst[m], map[m] (original entry -> relabeled entry),
+ * oldid[n] (new id -> original id).  ACCX_ERR_NOT_READY before accx_graph_relabel.
+ * No reference counterpart: the reference keeps its reorder maps internal
+ * (scan-query/util/graph.cpp:176-216). */
+int accx_graph_relabeled_csr(const accx_graph *g, uint32_t *roff, int32_t *rdst, uint32_t *map, uint32_t *oldid,
+                             void *stream);
+
 /* Copies the CSR back (host or device destination pointers). */
 int accx_graph_download(const accx_graph *g, uint32_t *off, int32_t *dst, void *stream);
 

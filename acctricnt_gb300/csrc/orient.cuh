@@ -170,9 +170,10 @@ __global__ void k_item_fill(const unsigned long long *__restrict__ icnt, const u
 // The slice is walked in rounds of blockDim entries; the classifier stored, per
 // bitmap entry (x,y), where P(y) starts and its length cut at min(x,y) (0 for
 // other entries), so a round starts with one coalesced load per entry.  Short
-// probe lists are concatenated (CTA prefix sum); long ones are cut into pieces
-// of LONG_PIECE ids; warps take short chunks and long pieces from one shared
-// queue, so no warp waits behind one long list.  A hit at partner entry j
+// probe lists are concatenated (CTA prefix sum) and cut into chunks; warps take
+// whole long lists (at most the owner counters' size, walked in pieces of
+// LONG_PIECE ids) and then the short chunks from one shared queue, so the
+// small grains even out the round's end.  A hit at partner entry j
 // credits cnt[j] (RED), the owner's shared counter of the id's rank, and the
 // edge (shared per-entry counters, credited after the round).
 // NT = the block size the per-round arrays are sized for (blockDim.x <= NT); a
@@ -194,10 +195,10 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bitmap_or(const uint32_t *__r
   uint32_t *ocnt = smem + nwords + 4;                              // pcap owner-prefix counters
   uint16_t *wbase = reinterpret_cast<uint16_t *>(ocnt + pcap);     // nwords first-id positions
   __shared__ unsigned long long s_it;
-  __shared__ uint32_t s_tot, s_nseg, s_nlong, s_nlp, s_next;
-  __shared__ uint32_t s_wsum[32], s_wcnt[32], s_wlong[32], s_wlp[32];
+  __shared__ uint32_t s_tot, s_nseg, s_nlong, s_next;
+  __shared__ uint32_t s_wsum[32], s_wcnt[32], s_wlong[32];
   __shared__ uint32_t s_pre[NT + 1], s_beg[NT], s_ent[NT], s_hit[NT];
-  __shared__ uint32_t s_lbeg[NT], s_llen[NT], s_lent[NT], s_lpc[NT + 1], s_lhit[NT];
+  __shared__ uint32_t s_lbeg[NT], s_llen[NT], s_lent[NT], s_lhit[NT];
   const int tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
   for (uint32_t i = tid; i <= nwords; i += nt) words[i] = 0;
@@ -238,38 +239,34 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bitmap_or(const uint32_t *__r
       probed += len;
       const bool is_short = len > 0 && len < LONG_SEG, is_long = len >= LONG_SEG;
       const unsigned bs = __ballot_sync(ACCX_FULL_MASK, is_short), bl = __ballot_sync(ACCX_FULL_MASK, is_long);
-      // long lists are cut into pieces on even entry boundaries (8-byte loads)
-      const uint32_t lp = is_long ? (len + (sst & 1u) + LONG_PIECE - 1) / LONG_PIECE : 0u;
-      uint32_t incl = is_short ? len : 0u, lincl = lp;
+      uint32_t incl = is_short ? len : 0u;
 #pragma unroll
       for (int d = 1; d < 32; d <<= 1) {
-        const uint32_t a = __shfl_up_sync(ACCX_FULL_MASK, incl, d), b = __shfl_up_sync(ACCX_FULL_MASK, lincl, d);
-        if (lane >= d) { incl += a; lincl += b; }
+        const uint32_t a = __shfl_up_sync(ACCX_FULL_MASK, incl, d);
+        if (lane >= d) incl += a;
       }
       if (lane == 31) {
         s_wsum[warp] = incl;
         s_wcnt[warp] = __popc(bs);
         s_wlong[warp] = __popc(bl);
-        s_wlp[warp] = lincl;
       }
       __syncthreads();
       if (warp == 0) {
         const uint32_t ws = lane < nwarps ? s_wsum[lane] : 0u, wc = lane < nwarps ? s_wcnt[lane] : 0u;
-        const uint32_t wl = lane < nwarps ? s_wlong[lane] : 0u, wp = lane < nwarps ? s_wlp[lane] : 0u;
-        uint32_t is = ws, ic = wc, il = wl, ip = wp;
+        const uint32_t wl = lane < nwarps ? s_wlong[lane] : 0u;
+        uint32_t is = ws, ic = wc, il = wl;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
           const uint32_t a = __shfl_up_sync(ACCX_FULL_MASK, is, d), b = __shfl_up_sync(ACCX_FULL_MASK, ic, d);
-          const uint32_t c = __shfl_up_sync(ACCX_FULL_MASK, il, d), q = __shfl_up_sync(ACCX_FULL_MASK, ip, d);
-          if (lane >= d) { is += a; ic += b; il += c; ip += q; }
+          const uint32_t c = __shfl_up_sync(ACCX_FULL_MASK, il, d);
+          if (lane >= d) { is += a; ic += b; il += c; }
         }
         if (lane < nwarps) {
           s_wsum[lane] = is - ws;
           s_wcnt[lane] = ic - wc;
           s_wlong[lane] = il - wl;
-          s_wlp[lane] = ip - wp;
         }
-        if (lane == 31) { s_tot = is; s_nseg = ic; s_nlong = il; s_nlp = ip; s_next = 0; }
+        if (lane == 31) { s_tot = is; s_nseg = ic; s_nlong = il; s_next = 0; }
       }
       __syncthreads();
       if (is_short) {
@@ -284,24 +281,21 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bitmap_or(const uint32_t *__r
         s_lbeg[idx] = sst;
         s_llen[idx] = len;
         s_lent[idx] = k;
-        s_lpc[idx] = s_wlp[warp] + lincl - lp;
         s_lhit[idx] = 0;
       }
-      if (tid == 0) {
-        s_pre[s_nseg] = s_tot;
-        s_lpc[s_nlong] = s_nlp;
-      }
+      if (tid == 0) s_pre[s_nseg] = s_tot;
       __syncthreads();
       const uint32_t tot = s_tot, nseg = s_nseg, nlong = s_nlong;
-      const uint32_t nsp = (tot + SHORT_PIECE - 1) / SHORT_PIECE, npieces = nsp + s_nlp;
+      // the queue: whole long lists first (the larger grains), then short chunks
+      const uint32_t nsp = (tot + SHORT_PIECE - 1) / SHORT_PIECE, npieces = nlong + nsp;
       for (;;) {
         uint32_t p = 0;
         if (lane == 0) p = atomicAdd(&s_next, 1u);
         p = __shfl_sync(ACCX_FULL_MASK, p, 0);
         if (p >= npieces) break;
-        if (p < nsp) {
+        if (p >= nlong) {
           // short chunk: SHORT_PIECE consecutive ids of the concatenation
-          const uint32_t c0 = p * SHORT_PIECE;
+          const uint32_t c0 = (p - nlong) * SHORT_PIECE;
           uint32_t lo = 0, hi = nseg;
           while (hi - lo > 1) {
             const uint32_t step = (hi - lo + 31) / 32;
@@ -341,47 +335,37 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bitmap_or(const uint32_t *__r
             }
           }
         } else {
-          // a piece of a long list: lane-consecutive ids, LONG_UNROLL loads in
-          // flight per lane; a warp's credits for one load land in one line of cnt
-          const uint32_t pl = p - nsp;
-          uint32_t lo = 0, hi = nlong;
-          while (hi - lo > 1) {
-            const uint32_t step = (hi - lo + 31) / 32;
-            const uint32_t q = lo + (uint32_t)lane * step;
-            const unsigned b = __ballot_sync(ACCX_FULL_MASK, q < hi && s_lpc[q] <= pl);
-            lo += (31 - __clz(b)) * step;
-            const uint32_t nh = lo + step;
-            hi = nh < hi ? nh : hi;
-          }
-          const uint32_t q = lo;
+          // a long list, walked in pieces of LONG_PIECE ids from the even entry at
+          // or before its start: lane pairs (j, j+1) come from one 8-byte load,
+          // ids outside [a0, a1) are dropped (the array's padding keeps the last
+          // pair in bounds); a warp's credits for one load land in one line of cnt
+          const uint32_t q = p;
           const uint32_t a0 = s_lbeg[q], a1 = a0 + s_llen[q];
-          // the piece spans [j0, j0 + LONG_PIECE) from the even entry at or before the
-          // list start; lane pairs (j, j+1) come from one 8-byte load, ids outside
-          // [a0, a1) are dropped (the array's padding keeps the last pair in bounds)
-          const uint32_t j0 = (a0 & ~1u) + (pl - s_lpc[q]) * LONG_PIECE;
-          int2 v[LONG_UNROLL / 2];
-#pragma unroll
-          for (int r = 0; r < LONG_UNROLL / 2; r++) {
-            const uint32_t j = j0 + 64u * r + 2u * (uint32_t)lane;
-            v[r] = j < a1 ? __ldg(reinterpret_cast<const int2 *>(dst + j)) : make_int2(-1, -1);
-            if (j < a0) v[r].x = -1;
-            if (j + 1u >= a1) v[r].y = -1;
-          }
-          // the warp stops at the first pair group past the list end (the last
-          // piece of a list is mostly shorter than LONG_PIECE)
-          const uint32_t rem = a1 - j0;
-          int32_t *const cl = cnt + j0 + 2u * (uint32_t)lane;
           uint32_t h = 0;
+          for (uint32_t j0 = a0 & ~1u; j0 < a1; j0 += LONG_PIECE) {
+            // all loads of a piece are issued (a test per load would serialise
+            // them); the probes stop at the first pair group past the list end
+            const uint32_t rem = a1 - j0;
+            int2 v[LONG_UNROLL / 2];
 #pragma unroll
-          for (int r = 0; r < LONG_UNROLL; r++) {
-            if (64u * (uint32_t)(r >> 1) >= rem) break;
-            const uint32_t id = min((uint32_t)((r & 1) ? v[r >> 1].y : v[r >> 1].x), W);
-            const uint32_t wd = words[id >> 5];
-            if ((wd >> (id & 31u)) & 1u) {
-              const uint32_t rk = wbase[id >> 5] + __popc(wd & ((1u << (id & 31u)) - 1u));
-              h++;
-              atomicAdd(cl + 64u * (r >> 1) + (uint32_t)(r & 1), 1);
-              if (rk < pxs) atomicAdd(&ocnt[rk], 1u);
+            for (int r = 0; r < LONG_UNROLL / 2; r++) {
+              const uint32_t j = j0 + 64u * r + 2u * (uint32_t)lane;
+              v[r] = j < a1 ? __ldg(reinterpret_cast<const int2 *>(dst + j)) : make_int2(-1, -1);
+              if (j < a0) v[r].x = -1;
+              if (j + 1u >= a1) v[r].y = -1;
+            }
+            int32_t *const cl = cnt + j0 + 2u * (uint32_t)lane;
+#pragma unroll
+            for (int r = 0; r < LONG_UNROLL; r++) {
+              if (64u * (uint32_t)(r >> 1) >= rem) break;
+              const uint32_t id = min((uint32_t)((r & 1) ? v[r >> 1].y : v[r >> 1].x), W);
+              const uint32_t wd = words[id >> 5];
+              if ((wd >> (id & 31u)) & 1u) {
+                const uint32_t rk = wbase[id >> 5] + __popc(wd & ((1u << (id & 31u)) - 1u));
+                h++;
+                atomicAdd(cl + 64u * (r >> 1) + (uint32_t)(r & 1), 1);
+                if (rk < pxs) atomicAdd(&ocnt[rk], 1u);
+              }
             }
           }
           h = __reduce_add_sync(ACCX_FULL_MASK, h);

@@ -159,6 +159,43 @@ __global__ void k_item_fill(const unsigned long long *__restrict__ icnt, const u
   }
 }
 
+// One piece of a long list for one warp: G pair groups (64 G ids) from the
+// even entry j0.  Lane pairs (j, j+1) come from one 8-byte load; ids outside
+// [a0, a1) are dropped (the array's padding keeps the last pair in bounds).
+// Every load is issued before the probes (a test per load would serialise
+// them); the probes stop at the first pair group past the list end.  A hit at
+// entry j credits cnt[j] -- a warp's credits for one load land in one line of
+// cnt -- and the owner counter of the id's rank; returns this lane's hits.
+template <int G>
+__device__ __forceinline__ uint32_t or_piece(const int32_t *__restrict__ dst, uint32_t j0, uint32_t a0, uint32_t a1,
+                                             uint32_t lane, uint32_t W, const uint32_t *words, const uint16_t *wbase,
+                                             uint32_t *ocnt, uint32_t pxs, int32_t *__restrict__ cnt) {
+  const uint32_t rem = a1 - j0;
+  int2 v[G];
+#pragma unroll
+  for (int r = 0; r < G; r++) {
+    const uint32_t j = j0 + 64u * r + 2u * lane;
+    v[r] = j < a1 ? __ldg(reinterpret_cast<const int2 *>(dst + j)) : make_int2(-1, -1);
+    if (j < a0) v[r].x = -1;
+    if (j + 1u >= a1) v[r].y = -1;
+  }
+  int32_t *const cl = cnt + j0 + 2u * lane;
+  uint32_t h = 0;
+#pragma unroll
+  for (int r = 0; r < 2 * G; r++) {
+    if (64u * (uint32_t)(r >> 1) >= rem) break;
+    const uint32_t id = min((uint32_t)((r & 1) ? v[r >> 1].y : v[r >> 1].x), W);  // W: the zero word
+    const uint32_t wd = words[id >> 5];
+    if ((wd >> (id & 31u)) & 1u) {
+      const uint32_t rk = wbase[id >> 5] + __popc(wd & ((1u << (id & 31u)) - 1u));
+      h++;
+      atomicAdd(cl + 64u * (r >> 1) + (uint32_t)(r & 1), 1);
+      if (rk < pxs) atomicAdd(&ocnt[rk], 1u);  // always true on a sorted CSR
+    }
+  }
+  return h;
+}
+
 #define SHORT_PIECE (32u * PROBE_UNROLL)  // ids per short piece (concatenated short lists)
 #define LONG_PIECE (32u * LONG_UNROLL)    // ids per piece of a long list
 
@@ -336,37 +373,18 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bitmap_or(const uint32_t *__r
           }
         } else {
           // a long list, walked in pieces of LONG_PIECE ids from the even entry at
-          // or before its start: lane pairs (j, j+1) come from one 8-byte load,
-          // ids outside [a0, a1) are dropped (the array's padding keeps the last
-          // pair in bounds); a warp's credits for one load land in one line of cnt
+          // or before its start
           const uint32_t q = p;
           const uint32_t a0 = s_lbeg[q], a1 = a0 + s_llen[q];
           uint32_t h = 0;
           for (uint32_t j0 = a0 & ~1u; j0 < a1; j0 += LONG_PIECE) {
-            // all loads of a piece are issued (a test per load would serialise
-            // them); the probes stop at the first pair group past the list end
+            // the last piece loads only the pair groups it needs (the size
+            // class is warp-uniform, and each class issues all its loads at once)
             const uint32_t rem = a1 - j0;
-            int2 v[LONG_UNROLL / 2];
-#pragma unroll
-            for (int r = 0; r < LONG_UNROLL / 2; r++) {
-              const uint32_t j = j0 + 64u * r + 2u * (uint32_t)lane;
-              v[r] = j < a1 ? __ldg(reinterpret_cast<const int2 *>(dst + j)) : make_int2(-1, -1);
-              if (j < a0) v[r].x = -1;
-              if (j + 1u >= a1) v[r].y = -1;
-            }
-            int32_t *const cl = cnt + j0 + 2u * (uint32_t)lane;
-#pragma unroll
-            for (int r = 0; r < LONG_UNROLL; r++) {
-              if (64u * (uint32_t)(r >> 1) >= rem) break;
-              const uint32_t id = min((uint32_t)((r & 1) ? v[r >> 1].y : v[r >> 1].x), W);
-              const uint32_t wd = words[id >> 5];
-              if ((wd >> (id & 31u)) & 1u) {
-                const uint32_t rk = wbase[id >> 5] + __popc(wd & ((1u << (id & 31u)) - 1u));
-                h++;
-                atomicAdd(cl + 64u * (r >> 1) + (uint32_t)(r & 1), 1);
-                if (rk < pxs) atomicAdd(&ocnt[rk], 1u);
-              }
-            }
+            if (rem > 256u) h += or_piece<LONG_UNROLL / 2>(dst, j0, a0, a1, lane, W, words, wbase, ocnt, pxs, cnt);
+            else if (rem > 128u) h += or_piece<4>(dst, j0, a0, a1, lane, W, words, wbase, ocnt, pxs, cnt);
+            else if (rem > 64u) h += or_piece<2>(dst, j0, a0, a1, lane, W, words, wbase, ocnt, pxs, cnt);
+            else h += or_piece<1>(dst, j0, a0, a1, lane, W, words, wbase, ocnt, pxs, cnt);
           }
           h = __reduce_add_sync(ACCX_FULL_MASK, h);
           if (lane == 0 && h) atomicAdd(&s_lhit[q], h);

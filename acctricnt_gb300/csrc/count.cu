@@ -60,8 +60,9 @@ __device__ __forceinline__ int accx_edge_kind(int policy, const uint8_t *table, 
 // prefix lengths pre[] in place of degrees; an edge whose smaller prefix is
 // empty closes no triangle from here and is left out; bitmap owners need an id
 // below bm_idlim (their prefix ids fit the dense window) and a prefix of at most
-// bm_pcap ids (the shared counters), otherwise their edges gallop (owner prefix
-// 16x the partner's or more) or merge.
+// bm_pcap ids (the shared counters), otherwise their edges gallop (the lanes
+// binary-search the partner's short prefix in the owner's; measured faster than
+// the warp merge for these low-degree owners at every degree ratio tried).
 template <int TILE, bool ORIENT>
 __global__ void __launch_bounds__(TILE) k_classify(const uint32_t *__restrict__ off, const uint32_t *__restrict__ tilerow, const int32_t *__restrict__ dst,
                                                    uint32_t n, uint32_t m, int policy,
@@ -90,9 +91,8 @@ __global__ void __launch_bounds__(TILE) k_classify(const uint32_t *__restrict__ 
       dv = pre[v];
       if (dv > 0 && accx_owns(u, du, v, dv)) {
         kind = accx_edge_kind(policy, s_table, du, dv);
-        // outside the window or the owner counters: galloping for uneven pairs, else merge
-        if (kind == ACCX_KIND_BITMAP && (u >= bm_idlim || du > bm_pcap))
-          kind = (du >= 16u * dv) ? ACCX_KIND_GALLOP : ACCX_KIND_MERGE;
+        // outside the window or the owner counters: galloping
+        if (kind == ACCX_KIND_BITMAP && (u >= bm_idlim || du > bm_pcap)) kind = ACCX_KIND_GALLOP;
       }
     } else {
       du = off[u + 1] - off[u];

@@ -25,7 +25,7 @@ def _all_orient(G, ref, bias=2):
     for pol in POLICIES:
         assert np.array_equal(G.count(policy=pol, bias=bias, orient=True), ref), pol
     assert np.array_equal(G.count(policy="table", table=_table(3), bias=bias, orient=True), ref)
-    # an 8192-id window and 256 owner counters: most bitmap owners fall back to merge
+    # an 8192-id window and 256 owner counters: most bitmap owners fall back to galloping
     assert np.array_equal(G.count(policy="bitmap", bias=bias, orient=True, window_kb=1, sparse_kb=1,
                                   block_warps=4), ref)
 

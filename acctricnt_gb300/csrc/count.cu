@@ -76,7 +76,12 @@ __global__ void __launch_bounds__(TILE) k_classify(const uint32_t *__restrict__ 
   // per-kind edges / work / owner-side sums of this CTA, added to the device
   // counters once per CTA (per-warp atomics on the same few words serialise in L2)
   __shared__ unsigned long long s_st[3 * ACCX_NUM_KINDS];
+  // merge / gallop list slots: counted per CTA, reserved with one device atomic
+  // per CTA and list (per-warp reservations serialise on the two counters)
+  __shared__ unsigned s_lcnt[2];
+  __shared__ unsigned long long s_lbase[2];
   if (threadIdx.x < 3 * ACCX_NUM_KINDS) s_st[threadIdx.x] = 0;
+  if (threadIdx.x < 2) s_lcnt[threadIdx.x] = 0;
   if (policy == ACCX_POLICY_TABLE || policy == ACCX_POLICY_MODEL)
     for (int i = threadIdx.x; i < ACCX_NB * ACCX_NB; i += TILE) s_table[i] = table[i];
   uint32_t base = blockIdx.x * (uint32_t)TILE;
@@ -119,6 +124,7 @@ __global__ void __launch_bounds__(TILE) k_classify(const uint32_t *__restrict__ 
   }
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
+  uint32_t lofs = 0;  // this entry's slot among the CTA's entries of its list
 #pragma unroll
   for (int k = 0; k < ACCX_NUM_KINDS; k++) {
     unsigned mask = __ballot_sync(ACCX_FULL_MASK, kind == k);
@@ -128,25 +134,16 @@ __global__ void __launch_bounds__(TILE) k_classify(const uint32_t *__restrict__ 
     unsigned long long wo = (kind == k && k != ACCX_KIND_BITMAP) ? du : 0;
     wo = __reduce_add_sync(ACCX_FULL_MASK, (unsigned)wo);
     int leader = __ffs(mask) - 1;
-    unsigned long long basepos = 0;
+    unsigned wbase = 0;
     if (lane == leader) {
       atomicAdd(&s_st[k], (unsigned long long)__popc(mask));
       atomicAdd(&s_st[ACCX_NUM_KINDS + k], w);
       if (wo) atomicAdd(&s_st[2 * ACCX_NUM_KINDS + k], wo);
-      if (k == ACCX_KIND_MERGE) basepos = atomicAdd(&ctr[C_MERGE], (unsigned long long)__popc(mask));
-      if (k == ACCX_KIND_GALLOP) basepos = atomicAdd(&ctr[C_GALLOP], (unsigned long long)__popc(mask));
+      if (k == ACCX_KIND_MERGE) wbase = atomicAdd(&s_lcnt[0], (unsigned)__popc(mask));
+      if (k == ACCX_KIND_GALLOP) wbase = atomicAdd(&s_lcnt[1], (unsigned)__popc(mask));
     }
-    basepos = __shfl_sync(ACCX_FULL_MASK, basepos, leader);
-    if (kind == k) {
-      uint32_t rank = __popc(mask & lt);
-      // owned edges number exactly m/2 on a symmetric graph; the guards only
-      // keep unvalidated asymmetric input inside the list
-      unsigned long long idx = basepos + rank;
-      if (idx < list_cap) {
-        if (k == ACCX_KIND_MERGE) list[idx] = make_uint2(u, e);
-        else if (k == ACCX_KIND_GALLOP) list[list_cap - 1 - idx] = make_uint2(u, e);
-      }
-    }
+    wbase = __shfl_sync(ACCX_FULL_MASK, wbase, leader);
+    if (kind == k) lofs = wbase + __popc(mask & lt);
     if (k == ACCX_KIND_BITMAP && kind == k) {
       // aggregate the owner's probe work per row before the atomic
       unsigned peers = __match_any_sync(mask, u);
@@ -157,6 +154,18 @@ __global__ void __launch_bounds__(TILE) k_classify(const uint32_t *__restrict__ 
   static_assert(C_WORK == C_EDGES + ACCX_NUM_KINDS && C_OWNER == C_WORK + ACCX_NUM_KINDS, "counter layout");
   __syncthreads();
   if (threadIdx.x < 3 * ACCX_NUM_KINDS && s_st[threadIdx.x]) atomicAdd(&ctr[C_EDGES + threadIdx.x], s_st[threadIdx.x]);
+  if (threadIdx.x < 2 && s_lcnt[threadIdx.x])
+    s_lbase[threadIdx.x] = atomicAdd(&ctr[threadIdx.x == 0 ? C_MERGE : C_GALLOP], (unsigned long long)s_lcnt[threadIdx.x]);
+  __syncthreads();
+  if (kind == ACCX_KIND_MERGE || kind == ACCX_KIND_GALLOP) {
+    // owned edges number exactly m/2 on a symmetric graph; the guard only keeps
+    // unvalidated asymmetric input inside the list
+    const unsigned long long idx = s_lbase[kind == ACCX_KIND_MERGE ? 0 : 1] + lofs;
+    if (idx < list_cap) {
+      if (kind == ACCX_KIND_MERGE) list[idx] = make_uint2(u, e);
+      else list[list_cap - 1 - idx] = make_uint2(u, e);
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------

@@ -322,6 +322,9 @@ __device__ __forceinline__ uint32_t accx_bm_test(const accx_bm_view &b, uint32_t
 
 #define PROBE_UNROLL 4
 #define LONG_SEG 64
+#ifndef GALLOP_OR_GROUP
+#define GALLOP_OR_GROUP 8  // lanes per galloping edge in oriented counts
+#endif
 
 // One CTA per virtual item (grid-stride).  Per round of up to blockDim owned
 // entries, each thread takes one entry (u,v) and the part of N(v) to probe.
@@ -733,7 +736,7 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s)
     k_merge_or<<<sms * 8, MERGE_WARPS * 32, 0, s>>>(off, dst, g->d_pre, g->d_rev, g->d_edge_list, list_cap, ctr,
                                                     cnt);
     ACCX_MARK(2);
-    k_gallop_or<<<sms * 8, MERGE_WARPS * 32, 0, s>>>(off, dst, g->d_pre, g->d_rev, g->d_edge_list, list_cap, ctr,
+    k_gallop_or<GALLOP_OR_GROUP><<<sms * 8, MERGE_WARPS * 32, 0, s>>>(off, dst, g->d_pre, g->d_rev, g->d_edge_list, list_cap, ctr,
                                                      cnt);
     ACCX_MARK(3);
     // blocks of up to 512 threads use the half-size instance (two CTAs per SM when

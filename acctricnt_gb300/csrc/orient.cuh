@@ -108,8 +108,12 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32) k_merge_or(const uint32_t *_
   if (lane == 0 && found) atomicAdd(&ctr[C_MATCH + ACCX_KIND_MERGE], found);
 }
 
-// Lanes take the partner's prefix ids in order and binary-search each in the
-// owner's prefix; every round starts at the position the last lane reached.
+// Groups of G lanes take one edge each: the lanes take the partner's prefix ids
+// in order and binary-search each in the owner's prefix; every round starts at
+// the position the group's last lane reached.  Galloping edges mostly have
+// short partner lists (the low-degree owners outside the bitmap window), so a
+// warp works on 32/G edges at once.
+template <int G>
 __global__ void __launch_bounds__(MERGE_WARPS * 32) k_gallop_or(const uint32_t *__restrict__ off,
                                                                  const int32_t *__restrict__ dst,
                                                                  const uint32_t *__restrict__ pre,
@@ -117,19 +121,23 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32) k_gallop_or(const uint32_t *
                                                                  const uint2 *__restrict__ list, uint32_t list_cap,
                                                                  unsigned long long *__restrict__ ctr,
                                                                  int32_t *__restrict__ cnt) {
+  static_assert(G == 8 || G == 16 || G == 32, "group size");
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int sub = lane / G, gl = lane % G;
+  const unsigned gmask = G == 32 ? ACCX_FULL_MASK : (((1u << G) - 1u) << (sub * G));
   unsigned long long found = 0;
   unsigned long long total = ctr[C_GALLOP];
   if (total > list_cap) total = list_cap;
-  const unsigned long long nw = (unsigned long long)gridDim.x * MERGE_WARPS;
-  for (unsigned long long it = (unsigned long long)blockIdx.x * MERGE_WARPS + w; it < total; it += nw) {
+  const unsigned long long ng = (unsigned long long)gridDim.x * MERGE_WARPS * (32 / G);
+  for (unsigned long long it = ((unsigned long long)blockIdx.x * MERGE_WARPS + w) * (32 / G) + sub; it < total;
+       it += ng) {
     const uint2 p = list[list_cap - 1 - it];
     const uint32_t x = p.x, e = p.y, y = (uint32_t)__ldg(dst + e);
     uint32_t xb, xe, yb, ye;
     accx_or_ranges(off, pre, rev, x, y, e, &xb, &xe, &yb, &ye);
     uint32_t c = 0, lo = xb;
-    for (uint32_t j0 = yb; j0 < ye && lo < xe; j0 += 32) {
-      const uint32_t j = j0 + (uint32_t)lane;
+    for (uint32_t j0 = yb; j0 < ye && lo < xe; j0 += G) {
+      const uint32_t j = j0 + (uint32_t)gl;
       uint32_t pos = xe;
       if (j < ye) {
         const int32_t id = __ldg(dst + j);
@@ -140,14 +148,15 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32) k_gallop_or(const uint32_t *
           atomicAdd(cnt + j, 1);
         }
       }
-      const uint32_t last_lane = (ye - j0 >= 32) ? 31u : (ye - j0 - 1);
-      lo = __shfl_sync(ACCX_FULL_MASK, pos, (int)last_lane);
+      const uint32_t last = (ye - j0 >= (uint32_t)G) ? (uint32_t)G - 1u : (ye - j0 - 1);
+      lo = __shfl_sync(gmask, pos, (int)last, G);
     }
-    c = __reduce_add_sync(ACCX_FULL_MASK, c);
-    if (lane == 0 && c) atomicAdd(cnt + (y < x ? e : ye), (int32_t)c);  // the edge's prefix entry
-    found += c;
+#pragma unroll
+    for (int d = G / 2; d >= 1; d >>= 1) c += __shfl_xor_sync(gmask, c, d, G);
+    if (gl == 0 && c) atomicAdd(cnt + (y < x ? e : ye), (int32_t)c);  // the edge's prefix entry
+    if (gl == 0) found += c;
   }
-  if (lane == 0 && found) atomicAdd(&ctr[C_MATCH + ACCX_KIND_GALLOP], found);
+  if (gl == 0 && found) atomicAdd(&ctr[C_MATCH + ACCX_KIND_GALLOP], found);
 }
 
 // items[i] = the owner of bitmap work item i (items of one owner are contiguous).

@@ -19,7 +19,9 @@
 // Included by count.cu after the shared counting definitions.
 #pragma once
 
-#define LONG_UNROLL 16  // loads in flight per lane on long probe lists (8 measured 4% slower, 4 25% slower)
+// ids per lane in a full piece of a long probe list (two per 8-byte load); at R-MAT
+// scale 24, 8 measured 4% slower
+#define LONG_UNROLL 16
 
 // pre[u] = |N(u) ∩ [0, u)|.
 __global__ void k_pre(const uint32_t *__restrict__ off, const int32_t *__restrict__ dst, uint32_t n,

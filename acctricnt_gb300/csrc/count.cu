@@ -322,7 +322,7 @@ __device__ __forceinline__ uint32_t accx_bm_test(const accx_bm_view &b, uint32_t
 
 #define PROBE_UNROLL 4  // ids per lane in a chunk of concatenated short lists
 // probe lists of at least LONG_SEG ids go whole to one warp, shorter ones are
-// concatenated; at R-MAT scale 24 the oriented kernel measured 32: +2%, 48: +0.7%, 128: +5.6%
+// concatenated; at R-MAT scale 24 the oriented kernel measured 32: +2.3%, 48: +0.7%, 128: +2.2%
 #define LONG_SEG 64
 #ifndef GALLOP_OR_GROUP
 #define GALLOP_OR_GROUP 8  // lanes per galloping edge in oriented counts (16: +24%, 32: +70% galloping time)

@@ -88,9 +88,12 @@ class ClockSampler:
          "clocks_event_reasons.sw_power_cap")
 
     def __init__(self, gpu_index):
+        import tempfile
         self.gpu = gpu_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench_%d.csv" % os.getpid())
+        # the raw samples go to ACCX_CLOCK_LOG_DIR when set (kept for inspection), else a temp folder
+        log_dir = os.environ.get("ACCX_CLOCK_LOG_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(log_dir, "clocks_bench_%d.csv" % os.getpid())
 
     def __enter__(self):
         try:

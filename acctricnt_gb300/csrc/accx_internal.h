@@ -4,6 +4,8 @@
 #include <stdint.h>
 #include <stdio.h>
 
+#include <atomic>
+
 #include "../../include/accx.h"
 
 #define ACCX_VERSION_STR "accx 0.1 sm_103a"
@@ -52,7 +54,9 @@ struct accx_graph {
   int32_t *d_cnt = nullptr;   // m
   float *d_simkey = nullptr;    // m: similarity key per entry (built by the first query after a count)
   uint32_t *d_src = nullptr;    // m: source vertex (row) of every entry, built with the keys
-  bool key_valid = false;
+  // set (release) once d_simkey/d_src hold the keys of the current counts; query
+  // threads read it (acquire) before using those arrays without the key lock
+  std::atomic<bool> key_valid{false};
   uint32_t *d_tilerow = nullptr;   // row of every 256-entry tile's first entry (+1 for the last entry)
   uint32_t *d_rtilerow = nullptr;  // the same for the relabeled CSR
   // degree-descending relabel (accx_graph_relabel): counting runs on these

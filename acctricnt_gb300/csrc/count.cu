@@ -787,7 +787,7 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s)
   g->cnt_valid = true;
   g->qc.query_valid = false;
   g->qc.pairs_valid = false;
-  g->key_valid = false;
+  g->key_valid.store(false, std::memory_order_release);
   return ACCX_OK;
 }
 

@@ -127,7 +127,7 @@ extern "C" int accx_cn_load(accx_graph *g, const char *path) {
   if (g->m) ACCX_CUDA_TRY(cudaMemcpy(g->d_cnt, h.data(), sizeof(int32_t) * g->m, cudaMemcpyHostToDevice));
   g->cnt_bias = hd.bias;
   g->cnt_valid = true;
-  g->key_valid = false;
+  g->key_valid.store(false, std::memory_order_release);
   g->qc.query_valid = false;
   g->qc.pairs_valid = false;
   return ACCX_OK;

@@ -24,8 +24,10 @@
 // so graphs up to 2 * ACCX_NOALLOC_MAX_OWNED CSR entries fit.
 #define ACCX_NOALLOC_MAX_OWNED (1u << 20)
 
-// [0, MAX): owned edges as (u, e); [MAX]: the list length (low 32 bits used as
-// an append counter, high bits unused).  8 MiB + 8 bytes per device.
+// [0, MAX): owned edges as (u, e); [MAX].x: the list length (an append
+// counter), [MAX].y: set to 1 when owned edges did not fit the list.  That can
+// only happen on an asymmetric CSR, which this entry point does not check: a
+// symmetric one has exactly m/2 owned edges.  8 MiB + 8 bytes per device.
 static __device__ __align__(256) uint2 g_noalloc_scratch[ACCX_NOALLOC_MAX_OWNED + 1];
 
 template <int TILE>
@@ -50,6 +52,7 @@ __global__ void __launch_bounds__(TILE) k_noalloc_classify(const uint32_t *__res
   if (own) {
     uint32_t idx = p + __popc(mask & ((1u << lane) - 1u));
     if (idx < ACCX_NOALLOC_MAX_OWNED) scratch[idx] = make_uint2(u, e);
+    else scratch[ACCX_NOALLOC_MAX_OWNED].y = 1u;  // dropped: asymmetric input
   }
 }
 
@@ -113,7 +116,8 @@ extern "C" int accx_cn_count_noalloc(const uint32_t *off, const int32_t *dst, ui
   if (rc) return rc;
   if (m == 0 || n == 0) return ACCX_OK;
   cudaStream_t s = (cudaStream_t)stream;
-  // the list length starts at zero on every call (the array keeps the last call's contents)
+  // the list length and the overflow flag start at zero on every call (the array
+  // keeps the last call's contents)
   ACCX_CUDA_TRY(cudaMemsetAsync(scratch + ACCX_NOALLOC_MAX_OWNED, 0, sizeof(uint2), s));
   const uint32_t m32 = (uint32_t)m;
   k_noalloc_classify<256><<<(m32 + 255) / 256, 256, 0, s>>>(off, dst, n, m32, scratch);

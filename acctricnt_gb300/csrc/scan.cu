@@ -384,12 +384,12 @@ extern "C" int accx_scan_query_ctx(const accx_graph *g, accx_query_ctx *q, doubl
   const int sms = accx_sm_count(g->device);
   ACCX_CUDA_TRY(cudaMemsetAsync(q->d_qcounters, 0, sizeof(unsigned long long) * Q_NUM, s));
   const uint32_t tiles = (m + 255) / 256;
-  if (m && !g->key_valid) {
+  if (m && !g->key_valid.load(std::memory_order_acquire)) {
     // once per count; several threads may query one const handle, so the key
     // array is built under a lock
     static std::mutex mu_key;
     std::lock_guard<std::mutex> lk(mu_key);
-    if (!g->key_valid) {
+    if (!g->key_valid.load(std::memory_order_relaxed)) {
       accx_graph *gm = const_cast<accx_graph *>(g);
       if (!gm->d_simkey) {
         ACCX_CUDA_TRY(accx_dev_alloc((void **)&gm->d_simkey, sizeof(float) * (size_t)m, g->home));
@@ -399,7 +399,7 @@ extern "C" int accx_scan_query_ctx(const accx_graph *g, accx_query_ctx *q, doubl
       k_simkey<256><<<tiles, 256, 0, s>>>(g->d_off, g->d_tilerow, g->d_dst, g->d_cnt, n, m, g->cnt_bias, gm->d_simkey,
                                           gm->d_src);
       ACCX_CUDA_TRY(cudaStreamSynchronize(s));
-      gm->key_valid = true;
+      gm->key_valid.store(true, std::memory_order_release);
     }
   }
   // threshold band on the keys: exact outside, simpred.h inside

@@ -235,50 +235,67 @@ def measure_e2e(G, policy, table, reps, models=None, orient=False):
                     "%s, host pinned out)" % (policy, "oriented" if orient else "direct")}
 
 
-class CpuSampler:
-    """Bounded samples of the oracle port of CheckCoreBitmap, scaled to the whole
-    count.  Owner work is very skewed (a few hubs own most probes), so owners are
-    ordered by their modelled work (oracle.owner_costs) and every stride-th one in
-    that order is timed; the whole count's time is estimated as sample time x
-    total work / sample work (a ratio estimator)."""
+CPU_STRIPES = 20  # a whole CPU count = this many stripes of CheckCoreBitmap's entry chunks
 
-    def __init__(self, off, dst, threads):
-        from oracle import oracle
-        self.oracle = oracle
-        self.off, self.dst, self.threads = off, dst, threads
-        self.n, self.m = len(off) - 1, len(dst)
-        self.cost = oracle.owner_costs(off, dst, threads).astype(np.float64)
-        self.order = np.argsort(self.cost, kind="stable").astype(np.uint32)
-        self.total = float(self.cost.sum())
-        self.cnn = np.full(max(self.m, 1), 2, np.int32)
 
-    def run(self, stride, start=0):
-        owners = np.sort(self.order[start % stride::stride])
+def cpu_orders(off, dst, threads):
+    """The CSR in the two vertex orders the reference's CPU build counts in:
+    "none" (as generated) and "deg" (its ReorderDegDescending, restated in the
+    oracle and run on the host; preprocessing, not timed)."""
+    from oracle import oracle
+    no, nd, _ = oracle.reorder_deg(off, dst, threads)
+    return {"none": (off, dst), "deg": (no, nd)}
+
+
+def spread_stripes(k):
+    """Stripe order that spreads any prefix over the whole count: 0, k/2, k/4, 3k/4, ..."""
+    order, seen = [], set()
+    step = k
+    while step >= 1:
+        for s in range(0, k, step):
+            if s not in seen:
+                seen.add(s)
+                order.append(s)
+        step //= 2
+    return order + [s for s in range(k) if s not in seen]
+
+
+def time_stripes(off, dst, cnn, stripes, nstripes, threads, budget_s=None):
+    """Times CheckCoreBitmap stripes (oracle restatement, all given threads) one
+    by one; stops early once budget_s is spent.  Returns (entries, seconds per stripe)."""
+    from oracle import oracle
+    entries, secs = 0, []
+    for s in stripes:
         t0 = time.perf_counter()
-        k, _ = self.oracle.cn_count_owners(self.off, self.dst, owners, self.threads, self.cnn)
-        dt = max(time.perf_counter() - t0, 1e-6)
-        frac = float(self.cost[owners].sum()) / self.total if self.total else 1.0
-        return {"dt": dt, "owners": len(owners), "owned": int(k), "frac": frac, "full_s": dt / max(frac, 1e-12)}
-
-    def calibrate(self, seconds):
-        """Stride whose sample takes about `seconds`."""
-        stride = max(1, self.n // 2048)
-        r = self.run(stride)
-        return max(1, min(self.n, int(stride * r["dt"] / max(seconds, 1e-3)))), r
-
-    def describe(self, stride):
-        return ("owners sorted by modelled work (2 d_u + sum of owned d_v + 8), every %d-th of %d timed; "
-                "whole-count time = sample time x total work / sample work" % (stride, self.n))
+        entries += oracle.cn_count_stripe(off, dst, cnn, s, nstripes, threads)
+        secs.append(time.perf_counter() - t0)
+        if budget_s is not None and sum(secs) >= budget_s:
+            break
+    return entries, secs
 
 
-def cpu_baseline(off, dst, budget_s, nthreads):
-    """Oracle port of CheckCoreBitmap on a work-stratified sample of owners."""
-    cs = CpuSampler(off, dst, nthreads)
-    stride, _ = cs.calibrate(budget_s / 2)
-    r = cs.run(stride, start=stride // 2)
-    return {"value": round(cs.m / r["full_s"] / 1e9, 5), "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": "%s: %d owners, %d owned edges, %.1f%% of the work, %.2f s -> %.1f s for the whole count"
-                      % (cs.describe(stride), r["owners"], r["owned"], 100 * r["frac"], r["dt"], r["full_s"])}
+def cpu_baseline(off, dst, budget_s, threads):
+    """The reference's CPU bitmap count (CheckCoreBitmap, restated in the oracle
+    with its entry chunks, schedule and bit vector) on the host cores, timed on
+    a bounded sample: stripes of its entry chunks (each 1/CPU_STRIPES of the
+    count, spread over the whole CSR), in both vertex orders, about budget_s/2
+    seconds each.  value = the CSR entries the timed stripes counted / their time;
+    the headline order is "deg", the reference's preferred order for this count."""
+    orders = cpu_orders(off, dst, threads)
+    res = {}
+    for name, (o, d) in orders.items():
+        cnn = np.full(max(len(d), 1), 2, np.int32)
+        k, secs = time_stripes(o, d, cnn, spread_stripes(CPU_STRIPES), CPU_STRIPES, threads, budget_s / 2)
+        res[name] = {"value": round(k / sum(secs) / 1e9, 5), "stripes": len(secs), "entries": int(k),
+                     "seconds": round(sum(secs), 2), "whole_count_s_estimate": round(sum(secs) * len(d) / k, 1)}
+    return {"value": res["deg"]["value"], "unit": UNIT, "cores": threads, "kind": "port", "order": "deg",
+            "orders": res,
+            "sample": "CheckCoreBitmap restated in C (OpenMP dynamic over 6000-entry chunks, per-thread bit "
+                      "vector), %d threads; timed stripes of its entry chunks (each 1/%d of the whole count, "
+                      "spread over the CSR); value = CSR entries counted / time; deg: %d stripes in %.1f s, "
+                      "none: %d stripes in %.1f s" % (threads, CPU_STRIPES, res["deg"]["stripes"],
+                                                      res["deg"]["seconds"], res["none"]["stripes"],
+                                                      res["none"]["seconds"])}
 
 
 def measured_regret(model_ms, alternatives):
@@ -310,6 +327,14 @@ def alg_bytes(G, dominant, stats, owner_work, matches=None):
     return 8 * G.m
 
 
+def workload_config(args, n, m, world):
+    """The `config` both arms print for the main workload."""
+    return {"workload": "R-MAT scale %d, edge factor %d, (0.57,0.19,0.19,0.05), seed 1+rank; all-edge CN count; "
+                        "SCAN eps %s mu %d" % (args.scale, args.edge_factor, list(QUERY_EPS), QUERY_MU),
+            "n": n, "m": m, "parallelism": "replicas%d" % world,
+            "l2": "inputs larger than L2 (CSR %.2f GB, counts %.2f GB)" % ((4 * m + 4 * n) / 1e9, 4 * m / 1e9)}
+
+
 def run_gb300(args):
     import torch
     from acctricnt_gb300 import accx
@@ -325,9 +350,10 @@ def run_gb300(args):
     table = None
     # correctness guard: the scheduled and plain counts are identical
     G.count(policy=policy, table=table, out=None, stream=sp, orient=orient)
-    a = G.count(policy=policy, table=table, stream=sp, orient=orient)
-    b = G.count(policy="heuristic", stream=sp)
+    a = G.count(policy=policy, table=table, stream=sp, orient=orient, bias=2)
+    b = G.count(policy="heuristic", stream=sp, bias=2)
     bit_exact = bool(np.array_equal(a, b))
+    count_sum = int(a.sum(dtype=np.int64))  # common_node_num summed (bias 2), as the reference arm prints
     del a, b
     with ClockSampler(local) as clk:
         ms, phases = time_counts(G, policy, table, args.steps, args.warmup, stream, world, orient=orient)
@@ -397,7 +423,7 @@ def run_gb300(args):
                 "merge_equiv_bytes": int(4 * float(np.sum(np.diff(G.download()[0]).astype(np.float64) ** 2)) + 4 * G.m)}
     e2e = None
     if not args.no_e2e and rank == 0:
-        e2e = measure_e2e(G, policy, table, 2, models, orient)
+        e2e = measure_e2e(G, policy, table, 5, models, orient)
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
         off, dst = G.download()
@@ -405,11 +431,9 @@ def run_gb300(args):
     line = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-            "config": {"workload": "R-MAT scale %d, edge factor %d, (0.57,0.19,0.19,0.05), seed 1+rank; all-edge CN "
-                                   "count; SCAN eps %s mu %d" % (args.scale, args.edge_factor, list(QUERY_EPS), QUERY_MU),
-                       "n": G.n, "m": G.m, "policy": policy, "orient": orient, "parallelism": "replicas%d" % world,
-                       "l2": "inputs larger than L2 (CSR %.2f GB, counts %.2f GB)" % ((4 * G.m + 4 * G.n) / 1e9,
-                                                                                   4 * G.m / 1e9)},
+            "config": workload_config(args, G.n, G.m, world),
+            "plan": {"policy": policy, "orient": orient},
+            "count_sum": count_sum,
             "plain": {"policy": "heuristic", "value": round(plain_value, 4), "ms_per_step": round(plain_ms, 3),
                       "phases_ms": {k: round(v, 3) for k, v in plain_phases.items()}},
             "speedup_vs_plain": round(plain_ms / ms, 3), "bit_exact_vs_plain": bit_exact,
@@ -427,39 +451,48 @@ def run_gb300(args):
             "sched": sched_info}
     if rank == 0:
         print(json.dumps(line), flush=True)
+    if not bit_exact:
+        sys.exit("scheduled and plain counts differ: the line above is not a valid measurement")
 
 
 def run_reference(args):
-    """The reference algorithm's CPU implementation on the host cores."""
+    """The reference algorithm's CPU implementation on the host cores: its
+    CheckCoreBitmap (restated in the oracle) with every host thread, on the
+    reference's degree-descending order of the same graph.  The count's entry
+    chunks are split into K = --steps stripes; each step counts one stripe, so
+    the K timed steps are exactly one whole count (W warm-up stripes run first
+    and are discarded).  value = m / the K steps' total time."""
     rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     if rank != 0:
         return
     from acctricnt_gb300 import accx
-    from oracle import oracle
     G = accx.Graph.generate(accx.rmat_params(args.scale, args.edge_factor, seed=1))
     off, dst = G.download()
+    n, m = G.n, G.m
     G.free()
-    n = len(off) - 1
     threads = os.cpu_count() or 1
-    # each step: a work-stratified sample of owners sized to about budget/steps seconds
-    cs = CpuSampler(off, dst, threads)
-    per_step = max(1.0, args.cpu_seconds / max(1, args.steps + args.warmup))
-    stride, _ = cs.calibrate(per_step)
-    est = []
-    for i in range(args.warmup + args.steps):
-        r = cs.run(stride, start=i)
-        if i >= args.warmup:
-            est.append(r["full_s"])
-    full_s = float(np.mean(est))
-    value = len(dst) / full_s / 1e9
-    line = {"metric": METRIC, "value": round(value, 5), "unit": UNIT, "impl": "reference", "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(full_s * 1e3, 3),
+    o, d = cpu_orders(off, dst, threads)["deg"]
+    del off, dst
+    K = max(1, args.steps)
+    cnn = np.full(max(m, 1), 2, np.int32)
+    time_stripes(o, d, cnn, [i % K for i in range(args.warmup)], K, threads)
+    cnn.fill(2)
+    entries, secs = time_stripes(o, d, cnn, range(K), K, threads)
+    assert entries == m, (entries, m)
+    total = sum(secs)
+    value = m / total / 1e9
+    line = {"metric": METRIC, "value": round(value, 5), "unit": UNIT, "impl": "reference", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total / K * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-            "config": {"workload": "R-MAT scale %d, edge factor %d, (0.57,0.19,0.19,0.05), seed 1; all-edge CN count"
-                                   % (args.scale, args.edge_factor), "n": n, "m": int(len(dst))},
-            "cpu_baseline": {"value": round(value, 5), "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": "per step: %s (CheckCoreBitmap restated in C, OpenMP, all host threads); "
-                                       "ms_per_step = estimated whole count" % cs.describe(stride)},
+            "config": workload_config(args, n, m, world),
+            "count_sum": int(cnn[:m].sum(dtype=np.int64)),
+            "cpu_baseline": {"value": round(value, 5), "unit": UNIT, "cores": threads, "kind": "port", "order": "deg",
+                             "sample": "the whole count: CheckCoreBitmap restated in C (OpenMP dynamic over "
+                                       "6000-entry chunks, per-thread bit vector), %d threads, on the reference's "
+                                       "degree-descending order; step i counts stripe i of %d (chunks c with "
+                                       "c %% %d == i), so the timed steps add up to one whole count, %.1f s"
+                                       % (threads, K, K, total)},
             "e2e": {"value": round(value, 5), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 

@@ -233,7 +233,10 @@ int accx_cn_last_timings(const accx_graph *g, float ms[ACCX_NUM_PHASES]);
  * stream-ordered pool budget, or a loop that must never enter the driver's
  * allocator.)  off/dst/cnt are device pointers: a symmetric CSR as
  * accx_graph_create accepts it, and the int32 output, cnt[e] = |N(u) ∩ N(v)| +
- * bias for every entry.  The only scratch is a fixed 8 MiB array inside the
+ * bias for every entry.  Precondition: the CSR is symmetric, sorted and free of
+ * self loops (validate it once with accx_graph_create and ACCX_GRAPH_VALIDATE);
+ * this call does not check it, and on an asymmetric CSR some entries of cnt are
+ * left unspecified while the call still returns ACCX_OK.  The only scratch is a fixed 8 MiB array inside the
  * library that every GPU loading the library keeps until the process exits, so
  * graphs are limited to accx_cn_count_noalloc_max_entries() CSR entries (2^21);
  * larger ones get ACCX_ERR_TOO_LARGE, host pointers ACCX_ERR_INVALID_ARG.  The

@@ -110,8 +110,15 @@ int oracle_cn_count(uint32_t n, const uint32_t *off, const int32_t *dst, int32_t
  * computed in the host's long double exactly as the reference does.  core_count
  * is accumulated per row (sequentially equal to the single-thread reference). */
 void oracle_similarity(uint32_t n, const uint32_t *off, const int32_t *dst, const int32_t *cnn, double eps,
-                       int mu, uint8_t *sim, int32_t *core_count, int32_t *label) {
-  for (uint32_t u = 0; u < n; u++) {
+                       int mu, uint8_t *sim, int32_t *core_count, int32_t *label, int nthreads) {
+  /* rows are independent (each row's core count is summed in entry order), so
+   * any thread count gives the single-thread result */
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 1024)
+#endif
+  for (int64_t ui = 0; ui < (int64_t)n; ui++) {
+    const uint32_t u = (uint32_t)ui;
     int32_t cc = 0;
     for (uint32_t e = off[u]; e < off[u + 1]; e++) {
       uint32_t v = (uint32_t)dst[e];
@@ -279,7 +286,7 @@ int64_t oracle_scan(uint32_t n, const uint32_t *off, const int32_t *dst, double 
                     const char *dir) {
   int rc = oracle_cn_count(n, off, dst, cnn, nthreads);
   if (rc) return rc;
-  oracle_similarity(n, off, dst, cnn, eps, mu, sim, core_count, label);
+  oracle_similarity(n, off, dst, cnn, eps, mu, sim, core_count, label, nthreads);
   oracle_cluster(n, off, dst, sim, label, cluster);
   int64_t k = oracle_noncore_pairs(n, off, dst, sim, label, cluster, NULL);
   int32_t *pairs = (int32_t *)malloc(sizeof(int32_t) * 2 * (size_t)(k ? k : 1));
@@ -301,62 +308,120 @@ void oracle_sim_batch(int64_t k, const uint32_t *cnn, const uint32_t *du, const 
   }
 }
 
-/* The CheckCoreBitmap work of a subset of owner vertices (a bounded sample of a
- * full count, used to time the CPU baseline): for each listed u, the owned
- * entries of u get cnn[e] = 2 + count and their reverse entries the same value.
- * Returns the number of owned edges processed (each fills two CSR entries). */
-int64_t oracle_cn_count_owners(uint32_t n, const uint32_t *off, const int32_t *dst, const uint32_t *owners,
-                               int64_t k, int nthreads, int32_t *cnn) {
-  int64_t done = 0;
+/* Row of CSR entry i, searched forward from row u (off[u] <= i): galloping, then
+ * a binary search, as FindSrc does (scan_xp.cpp:94-110); returns the last row r
+ * with off[r] <= i, which skips empty rows. */
+static uint32_t orc_find_src(const uint32_t *off, uint32_t n, uint32_t u, uint64_t i) {
+  if (i < off[u + 1]) return u;
+  uint32_t lo = u + 1, step = 1, hi = lo;
+  while (hi < n && off[hi + 1] <= i) { lo = hi + 1; hi = lo + step; step <<= 1; if (hi > n) hi = n; }
+  if (hi > n) hi = n;
+  /* first r in [lo, hi] with off[r + 1] > i */
+  while (lo < hi) {
+    uint32_t mid = lo + (hi - lo) / 2;
+    if (off[mid + 1] <= i) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+/* CheckCoreBitmap (scan_xp.cpp:219-337, the BIT_VEC build) over a stripe of its
+ * entry chunks: the reference walks the CSR entries in chunks of `chunk` (6000,
+ * OpenMP schedule(dynamic, 6000)); every thread keeps a bit vector of the
+ * neighbours of its current row u, rebuilt (old bits cleared) when the row
+ * changes; for an entry e = (u,v) that u owns (larger degree, ties: smaller id)
+ * it counts the set bits over N(v), adds the count to cnn[e] (which starts at
+ * 2) and copies cnn[e] to the reverse entry, found by binary search in N(v).
+ * This call processes the chunks c with c % nstripes == stripe, dynamically over
+ * nthreads threads, so nstripes calls (stripe 0..nstripes-1) are one whole
+ * count and each is a bounded, evenly spread part of it (the timed CPU
+ * baseline).  Returns the CSR entries in the stripe's chunks, -4 on an
+ * asymmetric graph. */
+int64_t oracle_cn_count_bitvec_stripe(uint32_t n, const uint32_t *off, const int32_t *dst, int32_t *cnn,
+                                      uint32_t chunk, uint32_t stripe, uint32_t nstripes, int nthreads) {
+  const uint64_t m = off[n];
+  if (chunk == 0 || nstripes == 0 || stripe >= nstripes) return -1;
+  const int64_t nchunks = (int64_t)((m + chunk - 1) / chunk);
+  const int64_t mine = nchunks > (int64_t)stripe ? (nchunks - (int64_t)stripe + nstripes - 1) / nstripes : 0;
+  const size_t words = ((size_t)n + 63) / 64;
+  int64_t entries = 0;
+  int bad = 0;
 #ifdef _OPENMP
   if (nthreads <= 0) nthreads = omp_get_max_threads();
-#pragma omp parallel num_threads(nthreads) reduction(+ : done)
+#pragma omp parallel num_threads(nthreads) reduction(+ : entries) reduction(| : bad)
 #endif
   {
-    uint8_t *bits = (uint8_t *)calloc(n ? n : 1, 1);
+    uint64_t *bits = (uint64_t *)calloc(words ? words : 1, sizeof(uint64_t));
+    uint32_t u = 0;
+    int64_t last_u = -1;
 #ifdef _OPENMP
-#pragma omp for schedule(dynamic, 16)
+#pragma omp for schedule(dynamic, 1)
 #endif
-    for (int64_t i = 0; i < k; i++) {
-      uint32_t u = owners[i];
-      uint32_t du = off[u + 1] - off[u];
-      for (uint32_t e = off[u]; e < off[u + 1]; e++) bits[dst[e]] = 1;
-      for (uint32_t e = off[u]; e < off[u + 1]; e++) {
-        uint32_t v = (uint32_t)dst[e];
-        uint32_t dv = off[v + 1] - off[v];
-        if (!(du > dv || (du == dv && u < v))) continue;
-        int32_t c = 0;
-        for (uint32_t f = off[v]; f < off[v + 1]; f++) c += bits[dst[f]];
-        cnn[e] = 2 + c;
-        uint32_t r = orc_binary_search(dst, off[v], off[v + 1], (int32_t)u);
-        if (r != UINT32_MAX) cnn[r] = cnn[e];
-        done++;
+    for (int64_t k = 0; k < mine; k++) {
+      const uint64_t c = (uint64_t)stripe + (uint64_t)k * nstripes;
+      const uint64_t e0 = c * chunk, e1 = e0 + chunk < m ? e0 + chunk : m;
+      entries += (int64_t)(e1 - e0);
+      if (off[u] > e0) u = 0; /* a chunk behind this thread's row: search from the start */
+      for (uint64_t i = e0; i < e1; i++) {
+        u = orc_find_src(off, n, u, i);
+        if ((int64_t)u != last_u) {
+          if (last_u >= 0)
+            for (uint32_t f = off[last_u]; f < off[last_u + 1]; f++) bits[(uint32_t)dst[f] >> 6] = 0;
+          for (uint32_t f = off[u]; f < off[u + 1]; f++) bits[(uint32_t)dst[f] >> 6] |= 1ull << ((uint32_t)dst[f] & 63);
+          last_u = u;
+        }
+        const uint32_t v = (uint32_t)dst[i];
+        const uint32_t du = off[u + 1] - off[u], dv = off[v + 1] - off[v];
+        if (du > dv || (du == dv && u < v)) {
+          int32_t cn = 0;
+          for (uint32_t f = off[v]; f < off[v + 1]; f++) cn += (int32_t)((bits[(uint32_t)dst[f] >> 6] >> ((uint32_t)dst[f] & 63)) & 1u);
+          cnn[i] += cn;
+          const uint32_t r = orc_binary_search(dst, off[v], off[v + 1], (int32_t)u);
+          if (r == UINT32_MAX) bad = 1; else cnn[r] = cnn[i];
+        }
       }
-      for (uint32_t e = off[u]; e < off[u + 1]; e++) bits[dst[e]] = 0;
     }
     free(bits);
   }
-  return done;
+  return bad ? -4 : entries;
 }
 
-/* Work of every owner in oracle_cn_count_owners, in list elements touched:
- * 2 d_u (bits set and cleared) + sum over owned v of (d_v + 8) (the probe of N(v)
- * and the reverse-entry search).  A sample of owners timed with that function
- * scales to the whole count by total cost / sample cost. */
-void oracle_owner_costs(uint32_t n, const uint32_t *off, const int32_t *dst, int nthreads, uint64_t *cost) {
+static int orc_int_cmp(const void *a, const void *b) {
+  const int32_t x = *(const int32_t *)a, y = *(const int32_t *)b;
+  return (x > y) - (x < y);
+}
+
+/* The reference's "deg" reorder, ReorderDegDescending + Reorder
+ * (scan_xp.cpp:1279-1301, :1145-1222): vertices sorted by degree, descending
+ * (old_vid[new] = old id; the reference's parallel sort leaves equal degrees in
+ * any order, this one keeps them by id), new_off from the new degrees, every
+ * row's ids mapped through new_vid and sorted.  Output arrays are caller-owned:
+ * new_off[n+1], new_dst[m], old_vid[n]. */
+void oracle_reorder_deg(uint32_t n, const uint32_t *off, const int32_t *dst, int nthreads, uint32_t *new_off,
+                        int32_t *new_dst, uint32_t *old_vid) {
+  uint32_t maxd = 0;
+  for (uint32_t u = 0; u < n; u++) if (off[u + 1] - off[u] > maxd) maxd = off[u + 1] - off[u];
+  /* counting sort by degree, descending, stable in the id */
+  uint64_t *start = (uint64_t *)calloc((size_t)maxd + 2, sizeof(uint64_t));
+  for (uint32_t u = 0; u < n; u++) start[maxd - (off[u + 1] - off[u]) + 1]++;
+  for (uint32_t d = 1; d <= maxd + 1; d++) start[d] += start[d - 1];
+  for (uint32_t u = 0; u < n; u++) old_vid[start[maxd - (off[u + 1] - off[u])]++] = u;
+  free(start);
+  uint32_t *new_vid = (uint32_t *)malloc(sizeof(uint32_t) * (n ? n : 1));
+  for (uint32_t i = 0; i < n; i++) new_vid[old_vid[i]] = i;
+  new_off[0] = 0;
+  for (uint32_t i = 0; i < n; i++) new_off[i + 1] = new_off[i] + (off[old_vid[i] + 1] - off[old_vid[i]]);
 #ifdef _OPENMP
   if (nthreads <= 0) nthreads = omp_get_max_threads();
-#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 1024)
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 100)
 #endif
-  for (int64_t i = 0; i < (int64_t)n; i++) {
-    const uint32_t u = (uint32_t)i, du = off[u + 1] - off[u];
-    uint64_t c = 2ull * du;
-    for (uint32_t e = off[u]; e < off[u + 1]; e++) {
-      const uint32_t v = (uint32_t)dst[e], dv = off[v + 1] - off[v];
-      if (du > dv || (du == dv && u < v)) c += (uint64_t)dv + 8u;
-    }
-    cost[u] = c;
+  for (int64_t ii = 0; ii < (int64_t)n; ii++) {
+    const uint32_t i = (uint32_t)ii, o = old_vid[i];
+    uint32_t k = new_off[i];
+    for (uint32_t f = off[o]; f < off[o + 1]; f++) new_dst[k++] = (int32_t)new_vid[(uint32_t)dst[f]];
+    const uint32_t len = new_off[i + 1] - new_off[i];
+    if (len > 1) qsort(new_dst + new_off[i], len, sizeof(int32_t), orc_int_cmp);
   }
+  free(new_vid);
 }
 
 /* ComputeVertexRangeAccumulatedFilteredDegree

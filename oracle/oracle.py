@@ -17,16 +17,18 @@ REF_HARNESS = os.path.join(HERE, "_ref", "ref_harness")
 REF_CLI = os.path.join(HERE, "_ref", "scan-xp-naive-bitvec")
 
 
-def build(ref_root="/root/reference"):
+def build(ref_root=None):
+    """make -C oracle; ref_root = the reference tree (None: the Makefile's
+    default); the reference build is skipped when the tree is absent."""
     args = ["make", "-s", "-C", HERE]
-    if ref_root:
+    if ref_root is not None:
         args.append("REF=" + ref_root)
     subprocess.run(args, check=True)
 
 
 def _load():
     if not os.path.exists(LIB_PATH):
-        build(ref_root=None)
+        build(ref_root=os.environ.get("ACCX_REFERENCE_ROOT", ""))
     lib = C.CDLL(LIB_PATH)
     P = C.c_void_p
     lib.oracle_check_graph.restype = C.c_int
@@ -34,7 +36,7 @@ def _load():
     lib.oracle_cn_count.restype = C.c_int
     lib.oracle_cn_count.argtypes = [C.c_uint32, P, P, P, C.c_int]
     lib.oracle_similarity.restype = None
-    lib.oracle_similarity.argtypes = [C.c_uint32, P, P, P, C.c_double, C.c_int, P, P, P]
+    lib.oracle_similarity.argtypes = [C.c_uint32, P, P, P, C.c_double, C.c_int, P, P, P, C.c_int]
     lib.oracle_cluster.restype = None
     lib.oracle_cluster.argtypes = [C.c_uint32, P, P, P, P, P]
     lib.oracle_noncore_pairs.restype = C.c_int64
@@ -43,10 +45,11 @@ def _load():
     lib.oracle_write_result.argtypes = [C.c_char_p, C.c_double, C.c_int, C.c_uint32, P, P, P, C.c_int64]
     lib.oracle_eps_string.restype = None
     lib.oracle_eps_string.argtypes = [C.c_double, C.c_char_p, C.c_int]
-    lib.oracle_cn_count_owners.restype = C.c_int64
-    lib.oracle_cn_count_owners.argtypes = [C.c_uint32, P, P, P, C.c_int64, C.c_int, P]
+    lib.oracle_cn_count_bitvec_stripe.restype = C.c_int64
+    lib.oracle_cn_count_bitvec_stripe.argtypes = [C.c_uint32, P, P, P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int]
     lib.oracle_vertex_ranges.restype = None
-    lib.oracle_owner_costs.argtypes = [C.c_uint32, P, P, C.c_int, P]
+    lib.oracle_reorder_deg.restype = None
+    lib.oracle_reorder_deg.argtypes = [C.c_uint32, P, P, C.c_int, P, P, P]
     lib.oracle_vertex_ranges.argtypes = [C.c_uint32, P, P, C.c_int, P]
     lib.oracle_sim_batch.restype = None
     lib.oracle_sim_batch.argtypes = [C.c_int64, P, P, P, C.c_double, P]
@@ -79,35 +82,42 @@ def cn_count(off, dst, nthreads=1):
     return cnn[:len(dst)]
 
 
-def cn_count_owners(off, dst, owners, nthreads=0, cnn=None):
-    """Counts the owned edges of the listed owner vertices only (a bounded sample
-    of the full count, for the timed CPU baseline).  Returns (owned edges
-    processed, cnn array)."""
+REF_CHUNK = 6000  # CheckCoreBitmap's OpenMP chunk of CSR entries (scan_xp.cpp:229)
+
+
+def cn_count_stripe(off, dst, cnn, stripe, nstripes, nthreads=0, chunk=REF_CHUNK):
+    """One stripe of CheckCoreBitmap's entry chunks (chunks c with c % nstripes ==
+    stripe), counted into cnn (int32[m], entries start at 2).  Stripes 0..nstripes-1
+    together are one whole count.  Returns the CSR entries of the stripe."""
     off, dst = _csr(off, dst)
-    owners = np.ascontiguousarray(owners, np.uint32)
-    if cnn is None:
-        cnn = np.full(max(len(dst), 1), 2, np.int32)
-    k = lib.oracle_cn_count_owners(len(off) - 1, _p(off), _p(dst), _p(owners), len(owners), int(nthreads), _p(cnn))
-    return int(k), cnn
+    assert cnn.dtype == np.int32 and cnn.flags.c_contiguous and len(cnn) >= len(dst)
+    k = lib.oracle_cn_count_bitvec_stripe(len(off) - 1, _p(off), _p(dst), _p(cnn), int(chunk), int(stripe),
+                                          int(nstripes), int(nthreads))
+    if k < 0:
+        raise RuntimeError("oracle_cn_count_bitvec_stripe failed: %d" % k)
+    return int(k)
 
 
-def owner_costs(off, dst, nthreads=0):
-    """Per-owner work of cn_count_owners (2 d_u + sum over owned v of d_v + 8), uint64[n]."""
+def reorder_deg(off, dst, nthreads=0):
+    """The reference's degree-descending reorder (ReorderDegDescending + Reorder):
+    returns (new_off, new_dst, old_vid) with old_vid[new id] = old id."""
     off, dst = _csr(off, dst)
     n = len(off) - 1
-    cost = np.zeros(max(n, 1), np.uint64)
-    lib.oracle_owner_costs(n, _p(off), _p(dst), int(nthreads), _p(cost))
-    return cost[:n]
+    new_off = np.zeros(n + 1, np.uint32)
+    new_dst = np.zeros(max(len(dst), 1), np.int32)
+    old_vid = np.zeros(max(n, 1), np.uint32)
+    lib.oracle_reorder_deg(n, _p(off), _p(dst), int(nthreads), _p(new_off), _p(new_dst), _p(old_vid))
+    return new_off, new_dst[:len(dst)], old_vid[:n]
 
 
-def similarity(off, dst, cnn, eps, mu):
+def similarity(off, dst, cnn, eps, mu, nthreads=1):
     off, dst = _csr(off, dst)
     n = len(off) - 1
     cnn = np.ascontiguousarray(cnn, np.int32)
     sim = np.zeros(max(len(dst), 1), np.uint8)
     cc = np.zeros(max(n, 1), np.int32)
     lab = np.zeros(max(n, 1), np.int32)
-    lib.oracle_similarity(n, _p(off), _p(dst), _p(cnn), float(eps), int(mu), _p(sim), _p(cc), _p(lab))
+    lib.oracle_similarity(n, _p(off), _p(dst), _p(cnn), float(eps), int(mu), _p(sim), _p(cc), _p(lab), int(nthreads))
     return sim[:len(dst)], cc[:n], lab[:n]
 
 
@@ -137,7 +147,13 @@ def scan(off, dst, eps, mu, nthreads=1, out_dir=None):
     """The whole reference pipeline; returns a dict of arrays (and writes the
     result file into out_dir when given)."""
     cnn = cn_count(off, dst, nthreads)
-    sim, cc, lab0 = similarity(off, dst, cnn, eps, mu)
+    return scan_from_counts(off, dst, cnn, eps, mu, nthreads, out_dir)
+
+
+def scan_from_counts(off, dst, cnn, eps, mu, nthreads=1, out_dir=None):
+    """The SCAN phases after the count (similarity, cores, clusters, hubs,
+    pairs, result file) on given common_node_num values."""
+    sim, cc, lab0 = similarity(off, dst, cnn, eps, mu, nthreads)
     lab, cl = cluster(off, dst, sim, lab0)
     pairs = noncore_pairs(off, dst, sim, lab, cl)
     if out_dir is not None:

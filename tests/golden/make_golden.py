@@ -12,7 +12,22 @@ reference's outputs: cnn (= 2 + common-neighbour count per CSR entry), sim,
 label (final, 0/1/2), cluster (min-id cluster of cores, -1 otherwise) and the
 bytes of its scanxp-result-<eps>-<mu>.txt file.  edge_list_converter.npz holds a
 text edge list and the two files the reference's converter writes for it.
+
+Two JSON fixtures too large to keep as arrays, or from another reference tool:
+  rmat16_e02_mu5_digests.json  the plain CPU config (R-MAT scale 16, edge factor
+      16, seed 1; eps 0.2, mu 5): sha256 digests (and sums) of the reference
+      build's cnn, sim, label and cluster arrays and of its result file;
+  vertex_ranges.json  the reference's ComputeVertexRangeAccumulatedFilteredDegree
+      ranges (oracle/_ref/ref_ranges) for every golden graph and R-MAT 16, at
+      several part counts.
+
+    python tests/golden/make_golden.py [npz] [converter] [digests] [ranges]
+
+(no argument: all of them).
 """
+import hashlib
+import json
+import subprocess
 import os
 import sys
 import tempfile
@@ -116,10 +131,68 @@ def edge_list_fixture():
         len(out["edges_txt"]), len(out["b_degree_bin"]), len(out["b_adj_bin"])))
 
 
+def sha256(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def plain_config_graph():
+    """R-MAT scale 16, edge factor 16, (0.57, 0.19, 0.19, 0.05), seed 1."""
+    return accx.generate_host(accx.rmat_params(16, 16, seed=1))
+
+
+def digests_fixture():
+    off, dst = plain_config_graph()
+    eps, mu = 0.2, 5
+    d = tempfile.mkdtemp(prefix="golden_dg_")
+    accx.write_graph_dir(d, off, dst)
+    ref = oracle.run_reference(d, eps, mu, os.path.join(d, "dump"))
+    fn = "scanxp-result-%s-%d.txt" % (oracle.eps_string(eps), mu)
+    with open(os.path.join(d, fn), "rb") as f:
+        result = f.read()
+    out = {"graph": "R-MAT scale 16, edge factor 16, (0.57,0.19,0.19,0.05), seed 1", "n": int(len(off) - 1),
+           "m": int(len(dst)), "eps": eps, "mu": mu, "graph_sha256": {"off": sha256(off), "dst": sha256(dst)},
+           "sha256": {k: sha256(ref[k]) for k in ("cnn", "sim", "label", "cluster")},
+           "sums": {k: int(ref[k].astype(np.int64).sum()) for k in ("cnn", "sim", "label", "cluster")},
+           "result_name": fn, "result_sha256": hashlib.sha256(result).hexdigest(), "result_bytes": len(result)}
+    with open(os.path.join(HERE, "rmat16_e02_mu5_digests.json"), "w") as f:
+        json.dump(out, f, indent=1)
+    print("rmat16_e02_mu5_digests    n=%d m=%d result=%d bytes" % (out["n"], out["m"], len(result)))
+
+
+RANGE_PARTS = (1, 2, 3, 4, 7, 8)
+
+
+def ranges_fixture():
+    exe = os.path.join(ROOT, "oracle", "_ref", "ref_ranges")
+    graphs = {name: (off, dst) for name, ((off, dst), _, _) in list(hand_graphs().items()) + list(seeded_graphs().items())}
+    graphs["rmat16"] = plain_config_graph()
+    out = {"parts": list(RANGE_PARTS), "ranges": {}}
+    for name, (off, dst) in sorted(graphs.items()):
+        d = tempfile.mkdtemp(prefix="golden_vr_")
+        accx.write_graph_dir(d, off, dst)
+        r = subprocess.run([exe, d] + [str(p) for p in RANGE_PARTS], check=True, capture_output=True, text=True)
+        out["ranges"][name] = [[int(x) for x in line.split()] for line in r.stdout.strip().splitlines()]
+    with open(os.path.join(HERE, "vertex_ranges.json"), "w") as f:
+        json.dump(out, f)
+    print("vertex_ranges             %d graphs x %d part counts" % (len(out["ranges"]), len(RANGE_PARTS)))
+
+
 def main():
+    what = set(sys.argv[1:]) or {"npz", "converter", "digests", "ranges"}
     oracle.build()
     if not oracle.have_reference():
         raise SystemExit("reference build not available; cannot regenerate fixtures")
+    if "digests" in what:
+        digests_fixture()
+    if "ranges" in what:
+        ranges_fixture()
+    if "npz" in what:
+        npz_fixtures()
+    if "converter" in what:
+        edge_list_fixture()
+
+
+def npz_fixtures():
     cases = {}
     cases.update(hand_graphs())
     cases.update(seeded_graphs())
@@ -136,7 +209,6 @@ def main():
         print("%-24s n=%-6d m=%-7d cores=%-5d hubs=%-4d pairs-lines=%d" % (
             name, len(off) - 1, len(dst), int((ref["label"] == 1).sum()), int((ref["label"] == 2).sum()),
             result.count(b"\nn ")))
-    edge_list_fixture()
 
 
 if __name__ == "__main__":

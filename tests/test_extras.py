@@ -10,6 +10,32 @@ if has_gpu():
 from oracle import oracle
 
 
+def _ranges_fixture():
+    import json
+    import os
+    from conftest import GOLDEN
+    with open(os.path.join(GOLDEN, "vertex_ranges.json")) as f:
+        return json.load(f)
+
+
+def _ranges_graph(name):
+    from acctricnt_gb300 import accx as ax
+    if name == "rmat16":
+        return ax.generate_host(ax.rmat_params(16, 16, seed=1))
+    g = load_golden(name)
+    return g["off"], g["dst"]
+
+
+@pytest.mark.parametrize("name", sorted(_ranges_fixture()["ranges"]))
+def test_oracle_vertex_ranges_equal_the_reference_partitioner(name):
+    """Ranges recorded from the reference's own
+    ComputeVertexRangeAccumulatedFilteredDegree (oracle/_ref/ref_ranges)."""
+    fx = _ranges_fixture()
+    off, dst = _ranges_graph(name)
+    for parts, want in zip(fx["parts"], fx["ranges"][name]):
+        assert oracle.vertex_ranges(off, dst, parts).tolist() == want, parts
+
+
 def test_oracle_vertex_ranges_cover_and_balance():
     from acctricnt_gb300 import accx as ax
     off, dst = ax.generate_host(ax.rmat_params(12, 16, seed=3))
@@ -54,8 +80,18 @@ def test_triangles_and_persistence(name, tmp_path):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(_ranges_fixture()["ranges"]))
+def test_vertex_ranges_equal_the_reference_partitioner(name):
+    fx = _ranges_fixture()
+    off, dst = _ranges_graph(name)
+    G = accx.Graph.from_csr(off, dst)
+    for parts, want in zip(fx["parts"], fx["ranges"][name]):
+        assert G.vertex_ranges(parts).tolist() == want, parts
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("parts", [1, 2, 3, 8])
-def test_vertex_ranges_equal_the_reference_partitioner(parts):
+def test_vertex_ranges_equal_the_oracle(parts):
     G = accx.Graph.generate(accx.rmat_params(16, 16, seed=5))
     off, dst = G.download()
     assert np.array_equal(G.vertex_ranges(parts), oracle.vertex_ranges(off, dst, parts))

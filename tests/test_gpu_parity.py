@@ -145,19 +145,57 @@ def test_large_rmat_policies_agree_and_are_symmetric():
         assert base[e] == len(np.intersect1d(a, b, assume_unique=True))
 
 
-def test_rmat24_full_size_properties():
+def test_plain_cpu_config_matches_reference_digests(tmp_path):
+    """R-MAT scale 16, edge factor 16, seed 1, eps 0.2, mu 5 (the plain CPU
+    config): every GPU output has the sha256 digest of the reference build's own
+    output (tests/golden/rmat16_e02_mu5_digests.json, from oracle/_ref/ref_harness),
+    for direct and oriented counts, relabeled or not."""
+    import hashlib
+    import json
+    from conftest import GOLDEN
+    with open(os.path.join(GOLDEN, "rmat16_e02_mu5_digests.json")) as f:
+        fx = json.load(f)
+    sha = lambda a: hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+    G = accx.Graph.generate(accx.rmat_params(16, 16, seed=1))
+    off, dst = G.download()
+    assert sha(off) == fx["graph_sha256"]["off"] and sha(dst) == fx["graph_sha256"]["dst"]
+    for kw in (dict(policy="heuristic"), dict(policy="bitmap"), dict(policy="bitmap", orient=True)):
+        assert sha(G.count(bias=2, **kw)) == fx["sha256"]["cnn"], kw
+    G.relabel()
+    for kw in (dict(policy="merge"), dict(policy="bitmap", orient=True), dict(policy="gallop", orient=True)):
+        assert sha(G.count(bias=2, **kw)) == fx["sha256"]["cnn"], kw
+    r = G.scan(fx["eps"], fx["mu"])
+    for k in ("sim", "label", "cluster"):
+        assert sha(r[k]) == fx["sha256"][k], k
+    G.write_result(str(tmp_path), fx["eps"], fx["mu"])
+    with open(os.path.join(str(tmp_path), fx["result_name"]), "rb") as f:
+        assert hashlib.sha256(f.read()).hexdigest() == fx["result_sha256"]
+
+
+def test_rmat24_full_parity_with_oracle():
     """The bench workload at full size, R-MAT scale 24 (16.8M vertices, 520.8M
-    entries): the oriented count on the relabeled copy equals the direct bitmap
-    count entry for entry; the counts' triangle total is an integer equal to
-    accx_triangles; 4096 sampled entries are symmetric and equal numpy set
+    entries): all counts of the oriented count on the relabeled copy (the bench's
+    plan) and of the reference's ratio-50 heuristic equal the oracle's
+    CheckCoreBitmap (all host threads) entry for entry, and the SCAN query's
+    similarity bits, labels, clusters and non-core pairs equal the oracle's at
+    eps 0.2, 0.5 and 0.8, mu 5.  Also: the triangle total is an integer equal to
+    accx_triangles, and 4096 sampled entries are symmetric and equal numpy set
     intersections on the caller's CSR."""
     G = accx.Graph.generate(accx.rmat_params(24, 16, seed=1))
     off, dst = G.download()
+    ref = oracle.cn_count(off, dst, nthreads=0)
+    assert np.array_equal(G.count(policy="heuristic", bias=2), ref)
     G.relabel()
-    direct = G.count(policy="bitmap", bias=2)
-    orient = G.count(policy="bitmap", bias=2, orient=True)
-    assert np.array_equal(orient, direct)
-    del orient
+    assert np.array_equal(G.count(policy="bitmap", bias=2, orient=True), ref)
+    for eps in (0.2, 0.5, 0.8):
+        want = oracle.scan_from_counts(off, dst, ref, eps, 5, nthreads=0)
+        r = G.scan(eps, 5)
+        assert np.array_equal(r["sim"], want["sim"]), eps
+        assert np.array_equal(r["label"], want["label"]), eps
+        assert np.array_equal(r["cluster"], want["cluster"]), eps
+        assert np.array_equal(G.pairs(), want["pairs"]), eps
+        del want, r
+    direct = ref
     s = int(direct.sum(dtype=np.int64)) - 2 * len(dst)
     assert s % 6 == 0 and G.triangles() == s // 6
     rng = np.random.default_rng(24)

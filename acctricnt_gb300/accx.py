@@ -89,6 +89,26 @@ class ServerStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+SCHED_NOFFSETS = 8
+
+
+class SchedConfig(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("epochs", C.c_int), ("lr", C.c_float), ("reps", C.c_int), ("quick", C.c_int)]
+
+
+class SchedInfo(C.Structure):
+    _fields_ = [("rows", C.c_uint32 * 2), ("loss_initial", C.c_float * 2), ("loss_final", C.c_float * 2),
+                ("bitmap_offset", C.c_float * 2), ("calib_relative", (C.c_float * SCHED_NOFFSETS) * 2),
+                ("collect_s", C.c_double * 2), ("train_s", C.c_double * 2), ("calibrate_s", C.c_double * 2),
+                ("quick", C.c_int)]
+
+
+class SchedPlan(C.Structure):
+    _fields_ = [("orient", C.c_int), ("predicted_ms", C.c_double * 2), ("calibrated_offset", C.c_float),
+                ("bitmap_offset", C.c_float), ("tuned", C.c_int), ("offsets", C.c_float * SCHED_NOFFSETS),
+                ("tune_ms", C.c_float * SCHED_NOFFSETS), ("tune_s", C.c_double)]
+
+
 def _load():
     if not os.path.exists(LIB_PATH):
         raise ImportError("libaccx.so not built (run __graft_entry__.build()): %s" % LIB_PATH)
@@ -163,6 +183,14 @@ def _load():
         "accx_batch_launch": (C.c_int, [P, P]),
         "accx_autotune": (C.c_int, [P, C.POINTER(CountOpts), C.c_int, C.POINTER(CountOpts), P, P, P, P]),
         "accx_similar_exact_batch": (C.c_int, [C.c_uint64, P, P, P, C.c_double, P]),
+        "accx_bucket_timings": (C.c_int, [P, C.c_int, C.c_int, C.c_uint64, P, P, P]),
+        "accx_sched_train": (C.c_int, [C.POINTER(SchedConfig), C.POINTER(P)]),
+        "accx_sched_free": (C.c_int, [P]),
+        "accx_sched_save": (C.c_int, [P, C.c_char_p]),
+        "accx_sched_load": (C.c_int, [C.c_char_p, C.POINTER(P)]),
+        "accx_sched_get_info": (C.c_int, [P, C.POINTER(SchedInfo)]),
+        "accx_sched_model": (C.c_int, [P, C.c_int, C.POINTER(P)]),
+        "accx_sched_plan_for": (C.c_int, [P, P, C.c_int, C.POINTER(CountOpts), C.POINTER(SchedPlan), P]),
     }
     for name, (res, args) in sigs.items():
         f = getattr(lib, name)
@@ -457,6 +485,15 @@ class Graph:
         _check(fn(self._h, _ptr(e), _ptr(so), _ptr(sp)), "bucket_stats")
         return e, so, sp
 
+    def bucket_timings(self, orient=False, reps=2, min_edges=1, stream=None):
+        """Per-bucket kernel timings (accx_bucket_timings): (edges[NB*NB],
+        ms[NB*NB, 3]) with NaN for buckets not timed."""
+        e = np.zeros(NB * NB, np.uint64)
+        t = np.zeros(NB * NB * 3, np.float32)
+        _check(lib.accx_bucket_timings(self._h, 1 if orient else 0, int(reps), int(min_edges), _ptr(e), _ptr(t),
+                                       _stream_ptr(stream)), "bucket_timings")
+        return e, t.reshape(NB * NB, 3).astype(np.float64)
+
     def bucket_features(self, orient=False):
         x = np.zeros((NB * NB, MODEL_IN), np.float32)
         fn = lib.accx_bucket_features_oriented if orient else lib.accx_bucket_features
@@ -498,13 +535,22 @@ class Model:
 
     def __init__(self, seed=1):
         self._h = C.c_void_p()
+        self._owner = None
         _check(lib.accx_model_create(int(seed), C.byref(self._h)), "model_create")
+
+    @classmethod
+    def _borrowed(cls, handle, owner):
+        """A model owned by a scheduler (freed with it)."""
+        m = cls.__new__(cls)
+        m._h = handle
+        m._owner = owner
+        return m
 
     def __del__(self):
         try:
-            if self._h:
+            if self._h and self._owner is None:
                 lib.accx_model_free(self._h)
-                self._h = None
+            self._h = None
         except Exception:
             pass
 
@@ -558,6 +604,78 @@ class Model:
         fn = lib.accx_model_table_for_oriented if orient else lib.accx_model_table_for
         _check(fn(self._h, graph._h, _ptr(t)), "model_table_for")
         return t.reshape(NB, NB)
+
+
+class Scheduler:
+    """The learned scheduler (accx_sched): a direct and an oriented cost model,
+    trained, calibrated, saved and planned by the library."""
+
+    def __init__(self, handle):
+        self._h = handle
+
+    @classmethod
+    def train(cls, seed=1, epochs=0, lr=0.0, reps=0, quick=False):
+        h = C.c_void_p()
+        cfg = SchedConfig(int(seed), int(epochs), float(lr), int(reps), 1 if quick else 0)
+        _check(lib.accx_sched_train(C.byref(cfg), C.byref(h)), "sched_train")
+        return cls(h)
+
+    @classmethod
+    def load(cls, path):
+        h = C.c_void_p()
+        _check(lib.accx_sched_load(path.encode(), C.byref(h)), "sched_load")
+        return cls(h)
+
+    def save(self, path):
+        _check(lib.accx_sched_save(self._h, path.encode()), "sched_save")
+
+    def free(self):
+        if self._h:
+            lib.accx_sched_free(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def model(self, orient=False):
+        h = C.c_void_p()
+        _check(lib.accx_sched_model(self._h, 1 if orient else 0, C.byref(h)), "sched_model")
+        return Model._borrowed(h, self)
+
+    def info(self):
+        i = SchedInfo()
+        _check(lib.accx_sched_get_info(self._h, C.byref(i)), "sched_get_info")
+        out = {}
+        for o, mode in enumerate(("direct", "oriented")):
+            out[mode] = {"rows": int(i.rows[o]), "loss_initial": round(float(i.loss_initial[o]), 4),
+                         "loss_final": round(float(i.loss_final[o]), 4),
+                         "bitmap_offset": float(i.bitmap_offset[o]),
+                         "calib_relative": [round(float(x), 4) for x in i.calib_relative[o]],
+                         "collect_s": round(i.collect_s[o], 2), "train_s": round(i.train_s[o], 2),
+                         "calibrate_s": round(i.calibrate_s[o], 2)}
+        out["quick"] = bool(i.quick)
+        return out
+
+    def plan(self, graph, tune=False, stream=None):
+        """Attaches both models to `graph` and picks the mode; returns a dict with
+        "policy" ("model"), "orient" and the predictions (and tuning times)."""
+        o = CountOpts()
+        p = SchedPlan()
+        _check(lib.accx_sched_plan_for(self._h, graph._h, 1 if tune else 0, C.byref(o), C.byref(p),
+                                       _stream_ptr(stream)), "sched_plan_for")
+        graph._model = self.model(False)
+        graph._model_or = self.model(True)
+        graph._sched = self
+        d = {"policy": "model", "orient": bool(p.orient),
+             "predicted_ms": {"direct": round(p.predicted_ms[0], 3), "oriented": round(p.predicted_ms[1], 3)},
+             "calibrated_offset": float(p.calibrated_offset), "bitmap_offset": float(p.bitmap_offset)}
+        if p.tuned:
+            d["tune"] = {"offsets": [float(x) for x in p.offsets], "candidate_ms": [round(float(x), 3) for x in p.tune_ms],
+                         "seconds": round(p.tune_s, 2)}
+        return d
 
 
 class Batch:

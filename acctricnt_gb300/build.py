@@ -19,7 +19,7 @@ BUILD = os.path.join(PKG, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 LIB = os.path.join(BUILD, "libaccx.so")
 CLIS = {"scan-xp-gb300": "main_scanxp.cpp", "scan-xp-gb300-varying": "main_scanxp_varying.cpp",
-        "edge-list-to-bins-gb300": "main_edgelist.cpp"}
+        "edge-list-to-bins-gb300": "main_edgelist.cpp", "accx-sched-train": "main_sched_train.cpp"}
 CLI = os.path.join(BUILD, "scan-xp-gb300")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

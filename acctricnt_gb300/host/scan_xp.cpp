@@ -7,6 +7,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <time.h>
+#include <unistd.h>
 
 #include <chrono>
 #include <stdexcept>
@@ -57,7 +58,23 @@ ScanXpOptions ScanXpOptions::from_env() {
   if (r) o.relabel = atoi(r) != 0;
   const char *q = getenv("ACCX_ORIENT");
   if (q) o.orient = atoi(q) != 0;
+  const char *m = getenv("ACCX_SCHED_MODEL");
+  if (m) o.sched_path = m;
+  const char *t = getenv("ACCX_SCHED_TUNE");
+  if (t) o.sched_tune = atoi(t) != 0;
   return o;
+}
+
+// <directory of this executable>/accx-sched.model: where the build puts the
+// scheduler file it trains.
+static std::string default_sched_path() {
+  char buf[4096];
+  const ssize_t k = readlink("/proc/self/exe", buf, sizeof(buf) - 1);
+  if (k <= 0) return "accx-sched.model";
+  buf[k] = 0;
+  std::string p(buf);
+  const size_t slash = p.rfind('/');
+  return (slash == std::string::npos ? std::string(".") : p.substr(0, slash)) + "/accx-sched.model";
 }
 
 // Default bucket table: galloping where the owner's degree bucket exceeds the
@@ -93,6 +110,7 @@ SCAN_XP::SCAN_XP(int thread_num, int min_u, double epsilon, char *dir, const Sca
 }
 
 SCAN_XP::~SCAN_XP() {
+  if (sched_) accx_sched_free(sched_);
   if (g_) accx_graph_free(g_);
 }
 
@@ -101,18 +119,32 @@ void SCAN_XP::CheckCore() {
   default_table(table);
   accx_count_opts o;
   memset(&o, 0, sizeof(o));
-  o.policy = opts_.policy;
-  o.table = table;
+  auto t0 = clk::now();
+  if (opts_.policy_set) {
+    o.policy = opts_.policy;
+    o.table = table;
+    o.orient = opts_.orient ? 1 : 0;
+    accx_log("kernel plan: policy %d from ACCX_POLICY (%s)", o.policy, o.orient ? "oriented" : "direct");
+  } else {
+    const std::string path = opts_.sched_path.empty() ? default_sched_path() : opts_.sched_path;
+    accx_sched_plan pl;
+    if (accx_sched_load(path.c_str(), &sched_) == ACCX_OK) {
+      check(accx_sched_plan_for(sched_, g_, opts_.sched_tune ? 1 : 0, &o, &pl, nullptr), "scheduler plan");
+      accx_log("kernel plan: learned scheduler %s -> %s counting (predicted %.3lf ms direct, %.3lf ms oriented; "
+               "bitmap offset %.2f)", path.c_str(), pl.orient ? "oriented" : "direct", pl.predicted_ms[0],
+               pl.predicted_ms[1], pl.bitmap_offset);
+    } else {
+      // the reference's fixed rule: ratio-50 galloping, else merge, full lists
+      o.policy = ACCX_POLICY_HEURISTIC;
+      o.orient = 0;
+      accx_log("kernel plan: reference ratio-50 rule (no scheduler file at %s)", path.c_str());
+    }
+  }
   o.bias = 2;  // common_node_num = 2 + |N(u) ∩ N(v)|
   o.block_warps = opts_.block_warps;
-  o.orient = opts_.orient ? 1 : 0;
-  // oriented counts without a chosen policy: the bitmap kind for every edge, the
-  // fastest fixed choice on skewed graphs (owners past the window fall back to merge)
-  if (opts_.orient && !opts_.policy_set && o.policy == ACCX_POLICY_TABLE) o.policy = ACCX_POLICY_BITMAP;
-  auto t0 = clk::now();
   check(accx_cn_count(g_, &o, nullptr, nullptr), "count");
   check(accx_scan_query(g_, epsilon_, min_u_, nullptr, nullptr, nullptr, &summary, nullptr), "similarity");
-  accx_log("All-Edge CN-Cnt + core checking (GPU, %s): %.3lf s", opts_.orient ? "oriented" : "direct", secs(t0));
+  accx_log("All-Edge CN-Cnt + core checking (GPU, %s): %.3lf s", o.orient ? "oriented" : "direct", secs(t0));
 }
 
 void SCAN_XP::ClusterCore() {

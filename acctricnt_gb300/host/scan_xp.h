@@ -14,13 +14,23 @@
 
 #include "accx.h"
 
+// How CheckCore picks its kernels.  Without an explicit policy it loads the
+// learned scheduler's file (accx_sched_load) and counts with the plan the
+// scheduler makes for the graph (mode and per-bucket kinds from the cost
+// models); when there is no usable file it falls back to the reference's own
+// rule, galloping iff one degree exceeds 50x the other, else merging, over full
+// lists (scan_xp_multi_gpu_multi_pass_common.cu:57-59, :105-117).  The counts
+// are the same either way.
 struct ScanXpOptions {
-  int policy = ACCX_POLICY_TABLE;  // counting policy (ACCX_POLICY_*); TABLE uses the default bucket table
-  bool policy_set = false;         // policy chosen by the caller (else oriented counts use the bitmap kind)
+  int policy = ACCX_POLICY_TABLE;  // explicit counting policy (ACCX_POLICY_*); TABLE uses the default bucket table
+  bool policy_set = false;         // a policy chosen by the caller (else: scheduler, or the ratio-50 fallback)
   bool relabel = true;             // count on the degree-descending relabeled copy
-  bool orient = true;              // oriented counting (triangle credits on prefix lists; same counts)
+  bool orient = true;              // with an explicit policy: oriented counting (same counts)
   int block_warps = 0;             // bitmap/merge CTA size in warps (0 = default)
-  // ACCX_POLICY=heuristic|merge|gallop|bitmap|table|model, ACCX_RELABEL=0|1, ACCX_ORIENT=0|1
+  std::string sched_path;          // scheduler file ("" = <directory of the executable>/accx-sched.model)
+  bool sched_tune = false;         // refine the bitmap offset on this graph (a whole count per candidate)
+  // ACCX_POLICY=heuristic|merge|gallop|bitmap|table|model, ACCX_RELABEL=0|1, ACCX_ORIENT=0|1,
+  // ACCX_SCHED_MODEL=<file>, ACCX_SCHED_TUNE=0|1
   static ScanXpOptions from_env();
 };
 
@@ -30,6 +40,7 @@ class SCAN_XP {
   double epsilon_;
   std::string dir_;
   accx_graph *g_ = nullptr;
+  accx_sched *sched_ = nullptr;
   ScanXpOptions opts_;
 
   void CheckCore();   // all-edge counts (+2 closed-neighbourhood bias) and cores

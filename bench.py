@@ -47,10 +47,15 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="rmat24", choices=["rmat24", "batch", "serve"])
+    ap.add_argument("--workload", default="rmat24", choices=["rmat24", "batch", "serve", "skew"],
+                    help="rmat24: the main line (with the skew, batch and serve results as extra keys unless "
+                         "--no-extras); the others print their own result alone")
+    ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--serve-scale", type=int, default=26)
     ap.add_argument("--serve-rate", type=float, default=10.0)
     ap.add_argument("--serve-requests", type=int, default=200)
+    ap.add_argument("--serve-rate-high", type=float, default=400.0)
+    ap.add_argument("--serve-requests-high", type=int, default=400)
     ap.add_argument("--serve-workers", type=int, default=4)
     ap.add_argument("--serve-budget-gb", type=float, default=64.0)
     ap.add_argument("--serve-check", type=int, default=40)
@@ -142,26 +147,24 @@ class ClockSampler:
 
 
 def pick_policy(G, args):
-    """The scheduled plan: two cost models (direct and oriented kernels, each
-    trained on the GPU from per-bucket kernel timings of small training graphs,
-    cached in the build folder) are attached to the graph; the mode whose model
-    predicts the smaller total time is chosen, and every count then runs the
-    register-resident inference kernel and classifies with its table on the
-    device.  Returns (policy, orient, {mode: model}, info)."""
+    """The scheduled plan (accx_sched_plan_for): the scheduler's two cost models
+    (direct and oriented kernels, trained on the GPU from per-bucket timings of
+    the plain kernels on small training graphs and calibrated on whole counts;
+    loaded from the build folder, else trained and saved there) are attached to
+    the graph, the mode whose model predicts the smaller total time is chosen,
+    and the chosen mode's bitmap offset is refined on this graph (one whole
+    count per candidate; preprocessing, like the relabel).  Every count then runs
+    the register-resident inference kernel and classifies with its table on the
+    device.  Returns (policy, orient, scheduler, info)."""
     if args.policy != "auto":
-        return args.policy, args.orient, {}, {}
+        return args.policy, args.orient, None, {}
     from acctricnt_gb300 import sched
     t0 = time.perf_counter()
-    md, info_d = sched.default_model(orient=False)
-    mo, info_o = sched.default_model(orient=True)
-    G.set_model(md)
-    G.set_model(mo, orient=True)
-    pl = sched.plan(G, md, mo)
-    info = {"direct_model": dict(info_d), "oriented_model": dict(info_o), "plan": pl,
-            "model_ready_s": round(time.perf_counter() - t0, 2)}
-    # the chosen mode's bitmap offset, refined on this graph (preprocessing, like the relabel)
-    info["offset_tune"] = sched.tune_offset(G, mo if pl["orient"] else md, orient=bool(pl["orient"]))
-    return "model", bool(pl["orient"]), {False: md, True: mo}, info
+    S, trained = sched.default_scheduler()
+    ready = time.perf_counter() - t0
+    pl = S.plan(G, tune=True)
+    info = {"scheduler": S.info(), "trained_now": trained, "model_ready_s": round(ready, 2), "plan": pl}
+    return "model", pl["orient"], S, info
 
 
 def time_counts(G, policy, table, steps, warmup, tstream, world, timing=True, orient=False):
@@ -205,34 +208,89 @@ def measure_queries(G, reps):
             "eps": list(QUERY_EPS), "mu": QUERY_MU}
 
 
-def measure_e2e(G, policy, table, reps, models=None, orient=False):
+def measure_e2e(G, policy, reps, sched=None, orient=False):
     """Through the C ABI with host buffers: pinned host CSR -> accx_graph_create
-    (copy + validation) -> relabel -> count -> counts copied back to pinned host
-    memory."""
+    (copy + validation) -> relabel -> the scheduler's plan (accx_sched_plan_for:
+    models attached, mode picked) -> count -> counts copied back to pinned host
+    memory.  Without a scheduler the count uses `policy` and `orient`."""
     import torch
     from acctricnt_gb300 import accx
     off, dst = G.download()
     t_off = torch.from_numpy(off.view(np.int32)).pin_memory()
     t_dst = torch.from_numpy(dst).pin_memory()
     t_cnt = torch.empty(G.m, dtype=torch.int32).pin_memory()
-    times = []
+    times, modes = [], set()
     for i in range(reps + 1):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         H = accx.Graph.from_device(t_off.data_ptr(), t_dst.data_ptr(), G.n, G.m, validate=True)
         H.relabel()
-        for mode, mdl in (models or {}).items():
-            H.set_model(mdl, orient=mode)
-        H.count(policy=policy, table=table, out=t_cnt.data_ptr(), orient=orient)
+        pol, ori = policy, orient
+        if sched is not None:
+            pl = sched.plan(H)
+            pol, ori = pl["policy"], pl["orient"]
+        H.count(policy=pol, out=t_cnt.data_ptr(), orient=ori)
         H.free()
         dt = time.perf_counter() - t0
+        modes.add("oriented" if ori else "direct")
         if i:
             times.append(dt)
     t = statistics.median(times)
     return {"value": round(G.m / t / 1e9, 4), "unit": UNIT, "h2d_bytes_per_step": 4 * (G.n + 1) + 4 * G.m,
-            "d2h_bytes_per_step": 4 * G.m, "ms_per_step": round(t * 1e3, 3),
-            "path": "accx_graph_create(host pinned CSR, validate) + accx_graph_relabel + accx_cn_count(%s policy, "
-                    "%s, host pinned out)" % (policy, "oriented" if orient else "direct")}
+            "d2h_bytes_per_step": 4 * G.m, "ms_per_step": round(t * 1e3, 3), "reps": reps,
+            "ms_all": [round(x * 1e3, 3) for x in times],
+            "path": "accx_graph_create(host pinned CSR, validate) + accx_graph_relabel + %saccx_cn_count(%s policy, "
+                    "%s, host pinned out)" % ("accx_sched_plan_for + " if sched is not None else "", policy,
+                                              "/".join(sorted(modes)))}
+
+
+# Fixed single policies a scheduled count is judged against: the reference's
+# ratio-50 rule ("plain") and each kernel kind for every edge, in both modes.
+# The direct merge kind for every edge is left out: on these graphs the ratio-50
+# rule already merges nearly every edge (the same work), and on 1M-degree hubs
+# (the power-law graph) merging full lists is quadratic.
+FIXED_POLICIES = (("direct_heuristic", "heuristic", False), ("direct_bitmap", "bitmap", False),
+                  ("direct_gallop", "gallop", False), ("oriented_merge", "merge", True),
+                  ("oriented_gallop", "gallop", True), ("oriented_bitmap", "bitmap", True))
+
+
+def time_fixed_policies(G, steps, stream, world, slow_ms=1500.0):
+    """Whole-count time (ms) of every fixed policy: one count first, then `steps`
+    timed counts when that one took less than slow_ms (else the single count)."""
+    out = {}
+    for name, pol, ori in FIXED_POLICIES:
+        first, _ = time_counts(G, pol, None, 1, 0, stream, world, timing=False, orient=ori)
+        if first < slow_ms:
+            first, _ = time_counts(G, pol, None, steps, 1, stream, world, timing=False, orient=ori)
+        out[name] = round(max_over_ranks(first, world), 3)
+    return out
+
+
+def judge_schedule(G, S, ms, orient, fixed, stream, world, steps):
+    """The scheduled count against the fixed policies and against the per-bucket
+    best table: measured regret, the other mode under its own model, and the
+    additive per-bucket estimate from buckets timed alone."""
+    from acctricnt_gb300 import accx, sched
+    sp = stream.cuda_stream
+    t0 = time.perf_counter()
+    other_ms, _ = time_counts(G, "model", None, steps, 1, stream, world, timing=False, orient=not orient)
+    edges, T = sched.bucket_timings(G, reps=1, stream=sp, orient=orient)
+    e, so, sp_ = G.bucket_stats(orient)
+    mt = S.model(orient).table_for(G, orient)
+    r = sched.regret(mt, edges, T)
+    best_tab = sched.exhaustive_table(edges, T).reshape(-1).copy()
+    best_tab[~np.isfinite(T).all(1)] = mt.reshape(-1)[~np.isfinite(T).all(1)]
+    best_ms, _ = time_counts(G, "table", best_tab, steps, 1, stream, world, timing=False, orient=orient)
+    bf = min(fixed, key=fixed.get)
+    return {"mode": "oriented" if orient else "direct", "other_mode_ms": round(other_ms, 3),
+            "fixed_ms": fixed, "best_fixed": {"policy": bf, "ms": fixed[bf],
+                                              "model_speedup": round(fixed[bf] / ms, 4)},
+            "speedup_vs_heuristic": round(fixed["direct_heuristic"] / ms, 3),
+            "best_table_count_ms": round(best_ms, 3),
+            "regret": measured_regret(ms, dict(fixed, per_bucket_best_table=best_ms)),
+            "bucket_regret_isolated": {k: round(v, 4) for k, v in r.items()},
+            "kinds_chosen": {k: int((mt.reshape(-1)[e > 0] == i).sum()) for i, k in enumerate(accx.KIND_NAMES)},
+            "judge_s": round(time.perf_counter() - t0, 2)}
 
 
 CPU_STRIPES = 20  # a whole CPU count = this many stripes of CheckCoreBitmap's entry chunks
@@ -346,7 +404,7 @@ def run_gb300(args):
     G.relabel(stream=sp)
     torch.cuda.synchronize()
     relabel_ms = (time.perf_counter() - t0) * 1e3
-    policy, orient, models, sched_info = pick_policy(G, args)
+    policy, orient, S, sched_info = pick_policy(G, args)
     table = None
     # correctness guard: the scheduled and plain counts are identical
     G.count(policy=policy, table=table, out=None, stream=sp, orient=orient)
@@ -361,36 +419,15 @@ def run_gb300(args):
     stats = G.last_stats()
     owner_work = G.owner_work()
     matches = G.last_matches() if orient else None
-    plain_ms, plain_phases = time_counts(G, "heuristic", None, args.steps, args.warmup, stream, world)
+    # the reference's fixed ratio-50 rule (direct) on the same GPU: a comparison
+    # line, so fewer steps (each count takes seconds)
+    plain_ms, plain_phases = time_counts(G, "heuristic", None, min(args.steps, 3), 1, stream, world)
     plain_ms = max_over_ranks(plain_ms, world)
-    bm_ms, _ = time_counts(G, "bitmap", None, max(1, args.steps // 2), 1, stream, world)
-    obm_ms, _ = time_counts(G, "bitmap", None, max(1, args.steps // 2), 1, stream, world, orient=True)
-    if models and args.regret and rank == 0:
-        from acctricnt_gb300 import sched
-        t0 = time.perf_counter()
-        # the other mode under its own model, measured: checks the mode choice
-        other_ms, _ = time_counts(G, policy, None, max(1, args.steps // 2), 1, stream, world, orient=not orient)
-        edges, T = sched.bucket_timings(G, reps=1, stream=sp, orient=orient)
-        e, so, sp_ = G.bucket_stats(orient)
-        mt = models[orient].table_for(G, orient)
-        r = sched.regret(mt, edges, T)
-        # the per-bucket best table, run as a whole count (the additive estimate checked)
-        best_tab = sched.exhaustive_table(edges, T).reshape(-1).copy()
-        best_tab[~np.isfinite(T).all(1)] = mt.reshape(-1)[~np.isfinite(T).all(1)]
-        best_ms, _ = time_counts(G, "table", best_tab, max(1, args.steps // 2), 1, stream, world, orient=orient)
-        sched_info.update({"mode": "oriented" if orient else "direct",
-                           "other_mode_ms": round(other_ms, 3),
-                           "best_table_count_ms": round(best_ms, 3),
-                           # regret of the scheduled count against the fastest whole count measured
-                           "regret": measured_regret(ms, {"per_bucket_best_table": best_ms,
-                                                          "oriented_bitmap_all": obm_ms,
-                                                          "direct_bitmap_all": bm_ms}),
-                           # additive estimate from buckets timed alone (biased against the bitmap kind)
-                           "bucket_regret_isolated": {k: round(v, 4) for k, v in r.items()},
-                           "heuristic_bucket_sum_ms": round(sched.table_time(sched.heuristic_table(e, so, sp_), T), 3),
-                           "bitmap_bucket_sum_ms": round(sched.table_time(np.full((24, 24), 2), T), 3),
-                           "exhaustive_timing_s": round(time.perf_counter() - t0, 2),
-                           "kinds_chosen": {k: int((mt.reshape(-1)[e > 0] == i).sum()) for i, k in enumerate(accx.KIND_NAMES)}})
+    judged = None
+    if S is not None and args.regret and rank == 0:
+        fixed = time_fixed_policies(G, max(1, args.steps // 2), stream, world)
+        fixed["direct_heuristic"] = round(plain_ms, 3)
+        judged = judge_schedule(G, S, ms, orient, fixed, stream, world, max(1, args.steps // 2))
     total_m = sum_over_ranks(G.m, world)
     value = total_m / (ms / 1e3) / 1e9
     plain_value = total_m / (plain_ms / 1e3) / 1e9
@@ -423,11 +460,12 @@ def run_gb300(args):
                 "merge_equiv_bytes": int(4 * float(np.sum(np.diff(G.download()[0]).astype(np.float64) ** 2)) + 4 * G.m)}
     e2e = None
     if not args.no_e2e and rank == 0:
-        e2e = measure_e2e(G, policy, table, 5, models, orient)
+        e2e = measure_e2e(G, policy, 5, S, orient)
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
         off, dst = G.download()
         cpu = cpu_baseline(off, dst, args.cpu_seconds, os.cpu_count() or 1)
+        del off, dst
     line = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int32", "data": "synthetic",
@@ -435,10 +473,8 @@ def run_gb300(args):
             "plan": {"policy": policy, "orient": orient},
             "count_sum": count_sum,
             "plain": {"policy": "heuristic", "value": round(plain_value, 4), "ms_per_step": round(plain_ms, 3),
-                      "phases_ms": {k: round(v, 3) for k, v in plain_phases.items()}},
+                      "steps": min(args.steps, 3), "phases_ms": {k: round(v, 3) for k, v in plain_phases.items()}},
             "speedup_vs_plain": round(plain_ms / ms, 3), "bit_exact_vs_plain": bit_exact,
-            "bitmap_all": {"ms_per_step": round(bm_ms, 3), "value": round(total_m / (bm_ms / 1e3) / 1e9, 4)},
-            "oriented_bitmap_all": {"ms_per_step": round(obm_ms, 3), "value": round(total_m / (obm_ms / 1e3) / 1e9, 4)},
             "relabel_ms": round(relabel_ms, 2),
             "phases_ms": {k: round(v, 3) for k, v in phases.items()}, "kinds": stats,
             "matches": ({"found": matches[0], "bitmap_probed": matches[1]} if matches else None),
@@ -448,11 +484,20 @@ def run_gb300(args):
             # counts, item fill, merge, gallop, bitmap, combine; gather back (relabeled graph)
             "gpu_launches": ((1 if policy == "model" else 0) + (9 if orient else 6) + 1) * args.steps,
             "clocks": clk.summary(),
-            "sched": sched_info}
+            "sched": dict(sched_info, **(judged or {}))}
+    G.free()
+    del G
+    if not args.no_extras and rank == 0 and world == 1:
+        line["skew"] = run_skew(args, S, stream)
+        line["batch"] = run_batch(args, S, stream)
+        line["serve"] = run_serve(args, S)
+    ok = bit_exact and all(line.get(k) is None or line[k].get("bit_exact", True) for k in ("skew", "batch"))
+    ok = ok and (line.get("serve") is None or line["serve"]["same_alone_and_mixed"]["identical"])
+    line["bit_exact"] = ok
     if rank == 0:
         print(json.dumps(line), flush=True)
-    if not bit_exact:
-        sys.exit("scheduled and plain counts differ: the line above is not a valid measurement")
+    if not ok:
+        sys.exit("counts differ between policies or from the oracle: the line above is not a valid measurement")
 
 
 def run_reference(args):
@@ -497,19 +542,62 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def run_batch(args):
+def run_skew(args, S, stream):
+    """The learned scheduler on skew: Chung-Lu (20M vertices, exponent 2.1, mean
+    degree 24, max expected degree 1M) and Erdos-Renyi (20M vertices, mean
+    degree 24), each relabeled and planned by the scheduler (mode + tuned
+    offset), against every fixed single policy on the same GPU; counts of the
+    scheduled plan equal the reference heuristic's bit for bit."""
+    import torch
+    from acctricnt_gb300 import accx, workloads
+    if S is None:
+        return None
+    out = {}
+    steps = max(3, args.steps // 4)
+    for name, params in (("chung_lu_20m", workloads.chung_lu_20m()), ("erdos_renyi_20m", workloads.er_20m())):
+        t0 = time.perf_counter()
+        G = accx.Graph.generate(params, stream=stream)
+        torch.cuda.synchronize()
+        gen_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        G.relabel(stream=stream.cuda_stream)
+        torch.cuda.synchronize()
+        relabel_ms = (time.perf_counter() - t0) * 1e3
+        pl = S.plan(G, tune=True, stream=stream)
+        orient = pl["orient"]
+        ms, phases = time_counts(G, "model", None, steps, 1, stream, 1, orient=orient)
+        a = G.count(policy="model", orient=orient, bias=2, stream=stream.cuda_stream)
+        b = G.count(policy="heuristic", bias=2, stream=stream.cuda_stream)
+        exact = bool(np.array_equal(a, b))
+        deg = np.diff(G.download()[0].astype(np.int64))
+        del a, b
+        fixed = time_fixed_policies(G, steps, stream, 1)
+        judged = judge_schedule(G, S, ms, orient, fixed, stream, 1, steps)
+        out[name] = {"n": G.n, "m": G.m, "max_degree": int(deg.max()), "gen_s": round(gen_s, 2),
+                     "relabel_ms": round(relabel_ms, 2), "plan": pl, "ms_per_step": round(ms, 3), "steps": steps,
+                     "value": round(G.m / (ms / 1e3) / 1e9, 4), "phases_ms": {k: round(v, 3) for k, v in phases.items()},
+                     "bit_exact": exact, **judged}
+        G.free()
+        del G
+    out["bit_exact"] = all(v["bit_exact"] for v in out.values() if isinstance(v, dict))
+    return out
+
+
+def run_batch(args, S, stream):
     """512 uneven graphs (log-uniform 1K-2M edge draws, R-MAT/ER mix): counts plus
     SCAN eps=0.3 mu=4 per graph, one captured launch sequence over their
-    disjoint union vs one count+query call sequence per graph."""
+    disjoint union vs one count+query call sequence per graph.  Every graph's
+    slice of the union counts must equal that graph's own count by the
+    reference's ratio-50 rule."""
     import torch
     from acctricnt_gb300 import accx, sched, workloads
-    rank, world, local = dist_setup(args)
-    params = workloads.batch_uneven(k=args.batch_k, seed=1 + rank)
+    params = workloads.batch_uneven(k=args.batch_k, seed=1)
     t0 = time.perf_counter()
     gs = [accx.Graph.generate(p) for p in params]
     gen_s = time.perf_counter() - t0
-    model, info = sched.default_model(orient=True)
-    stream = torch.cuda.Stream()
+    if S is None:
+        S, _ = sched.default_scheduler()
+    model = S.model(True)
     sp = stream.cuda_stream
     total_m = sum(G.m for G in gs)
     # one call sequence per graph (each graph relabeled and counted on its own)
@@ -552,59 +640,32 @@ def run_batch(args):
     torch.cuda.synchronize()
     batch_ms = ev0.elapsed_time(ev1) / args.steps
     wall_ms = (time.perf_counter() - t0) / args.steps * 1e3
-    exact = all(np.array_equal(c, G.count(policy="heuristic")) for c, G in
-                zip(B.split(U.read_counts()), gs[:32]))
-    line = {"metric": "batched all-edge CN + SCAN Gedges/s (%d uneven graphs)" % len(gs),
-            "value": round(total_m / (max(batch_ms, wall_ms) / 1e3) / 1e9, 4), "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(max(batch_ms, wall_ms), 3),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-            "config": {"workload": "%d graphs, undirected edge draws log-uniform 1K-2M, R-MAT scale 10-18 / ER mix, "
-                                   "seed %d; counts + SCAN eps 0.3 mu 4 per graph" % (len(gs), 1 + rank),
-                       "n": U.n, "m": total_m, "gen_s": round(gen_s, 2)},
-            "per_graph": {"ms_per_step": round(per_ms, 3), "value": round(total_m / (per_ms / 1e3) / 1e9, 4)},
-            "speedup_vs_per_graph": round(per_ms / max(batch_ms, wall_ms), 3), "bit_exact": bool(exact),
-            "autotune": {"chosen": kw, "ms": round(tune_ms, 3), "all_ms": [round(x, 3) for x in tune_all]},
-            "gpu_launches": "captured count (1 graph launch) + one SCAN query per step"}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    # every graph: its slice of the captured union count == its own ratio-50 count
+    bad = [i for i, (c, G) in enumerate(zip(B.split(U.read_counts()), gs))
+           if not np.array_equal(c, G.count(policy="heuristic"))]
+    step_ms = max(batch_ms, wall_ms)
+    res = {"metric": "batched all-edge CN + SCAN Gedges/s (%d uneven graphs)" % len(gs),
+           "value": round(total_m / (step_ms / 1e3) / 1e9, 4), "unit": UNIT, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": round(step_ms, 3),
+           "workload": "%d graphs, undirected edge draws log-uniform 1K-2M, R-MAT scale 10-18 / ER mix, seed 1; "
+                       "counts + SCAN eps 0.3 mu 4 per graph" % len(gs),
+           "n": U.n, "m": total_m, "gen_s": round(gen_s, 2),
+           "per_graph": {"ms_per_step": round(per_ms, 3), "value": round(total_m / (per_ms / 1e3) / 1e9, 4)},
+           "speedup_vs_per_graph": round(per_ms / step_ms, 3),
+           "bit_exact": not bad, "checked_graphs": len(gs), "mismatched_graphs": bad[:8],
+           "autotune": {"chosen": kw, "ms": round(tune_ms, 3), "all_ms": [round(x, 3) for x in tune_all]},
+           "gpu_launches_per_step": "one captured CUDA graph (the count) + one SCAN query"}
+    B.free()
+    for G in gs:
+        G.free()
+    return res
 
 
-def run_serve(args):
-    """Serving: a resident counted R-MAT graph; a Poisson stream of SCAN queries
-    (eps ~ U[0.1, 0.9], mu ~ U{2..20}) mixed with new-graph count requests
-    (R-MAT scale U{14..22}), admitted by an HBM budget."""
-    import torch
-    from acctricnt_gb300 import accx, sched
-    rank, world, local = dist_setup(args)
-    t0 = time.perf_counter()
-    G = accx.Graph.generate(accx.rmat_params(args.serve_scale, 16, seed=1 + rank))
-    torch.cuda.synchronize()
-    gen_s = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    G.relabel()
-    model, info = sched.default_model(orient=True)
-    G.set_model(model, orient=True)
-    G.count(policy="model", out=None, orient=True)
-    torch.cuda.synchronize()
-    count_s = time.perf_counter() - t0
-    rng = np.random.default_rng(7 + rank)
-    reqs = []
-    for i in range(args.serve_requests):
-        if rng.random() < args.count_frac:
-            reqs.append(accx.count_request(accx.rmat_params(int(rng.integers(14, 23)), 16, seed=1000 + i)))
-        else:
-            reqs.append(accx.query_request(float(rng.uniform(0.1, 0.9)), int(rng.integers(2, 21))))
-    gaps = rng.exponential(1.0 / args.serve_rate, len(reqs))
-    S = accx.Server(G, workers=args.serve_workers, hbm_budget=int(args.serve_budget_gb * (1 << 30)),
-                    count_policy="bitmap", count_orient=True)
-    for r in reqs[:4]:  # warm each path once (contexts, per-graph arrays)
-        S.wait(S.submit(r))
-    S.close()
-    S = accx.Server(G, workers=args.serve_workers, hbm_budget=int(args.serve_budget_gb * (1 << 30)),
-                    count_policy="bitmap", count_orient=True)
+def _serve_point(G, reqs, gaps, workers, budget):
+    from acctricnt_gb300 import accx
+    S = accx.Server(G, workers=workers, hbm_budget=budget, count_policy="bitmap", count_orient=True)
     ids = []
-    t_start = time.perf_counter()
-    t_next = t_start
+    t_next = time.perf_counter()
     for r, gap in zip(reqs, gaps):
         t_next += gap
         while time.perf_counter() < t_next:
@@ -614,9 +675,68 @@ def run_serve(args):
     res = [S.wait(i) for i in ids]
     st = S.stats()
     S.close()
-    # the same requests alone, one at a time: results must be identical
+    return res, st
+
+
+def run_serve(args, S=None):
+    """Serving: a resident counted R-MAT graph; a Poisson stream of SCAN queries
+    (eps ~ U[0.1, 0.9], mu ~ U{2..20}) mixed with new-graph count requests
+    (R-MAT scale U{14..22}), admitted by an HBM budget.  Two load points: the
+    configured rate, and a saturating one at which every worker is busy; the
+    first requests of the saturated mix are run again alone, one at a time, and
+    must give identical results."""
+    import torch
+    from acctricnt_gb300 import accx, sched
+    t0 = time.perf_counter()
+    G = accx.Graph.generate(accx.rmat_params(args.serve_scale, 16, seed=1))
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    G.relabel()
+    if S is None:
+        S, _ = sched.default_scheduler()
+    G.set_model(S.model(True), orient=True)
+    G.count(policy="model", out=None, orient=True)
+    torch.cuda.synchronize()
+    count_s = time.perf_counter() - t0
+    budget = int(args.serve_budget_gb * (1 << 30))
+
+    def requests(n, seed):
+        rng = np.random.default_rng(seed)
+        reqs = []
+        for i in range(n):
+            if rng.random() < args.count_frac:
+                reqs.append(accx.count_request(accx.rmat_params(int(rng.integers(14, 23)), 16, seed=1000 + i)))
+            else:
+                reqs.append(accx.query_request(float(rng.uniform(0.1, 0.9)), int(rng.integers(2, 21))))
+        return reqs, rng
+
+    warm, _ = requests(8, 99)
+    W = accx.Server(G, workers=args.serve_workers, hbm_budget=budget, count_policy="bitmap", count_orient=True)
+    for r in warm:  # warm each path once (contexts, per-graph arrays)
+        W.wait(W.submit(r))
+    W.close()
+    pct = lambda v, p: round(v[min(len(v) - 1, int(round(p * (len(v) - 1))))], 3) if v else None
+    points = {}
+    mixed = None
+    for label, rate, n in (("light", args.serve_rate, args.serve_requests),
+                           ("saturated", args.serve_rate_high, args.serve_requests_high)):
+        reqs, rng = requests(n, 7)
+        gaps = rng.exponential(1.0 / rate, len(reqs))
+        res, st = _serve_point(G, reqs, gaps, args.serve_workers, budget)
+        qrun = sorted(r.run_ms for r in res if r.type == accx.REQ_QUERY)
+        points[label] = {"rate_rps": rate, "requests": n,
+                         "query": {"p50_ms": st["query_p50_ms"], "p99_ms": st["query_p99_ms"],
+                                   "run_p50_ms": pct(qrun, 0.5), "run_p99_ms": pct(qrun, 0.99), "n": len(qrun)},
+                         "count": {"p50_ms": st["count_p50_ms"], "p99_ms": st["count_p99_ms"],
+                                   "n": sum(1 for r in res if r.type == accx.REQ_COUNT)},
+                         "throughput_rps": round(st["throughput_rps"], 2), "max_concurrent": st["max_concurrent"],
+                         "peak_budget_gb": round(st["peak_bytes"] / (1 << 30), 2), "failed": st["failed"]}
+        mixed = (reqs, res)
+    # the saturated mix's first requests alone, one at a time: results must be identical
+    reqs, res = mixed
     k = min(len(reqs), args.serve_check)
-    A = accx.Server(G, workers=1, hbm_budget=int(args.serve_budget_gb * (1 << 30)), count_policy="bitmap")
+    A = accx.Server(G, workers=1, hbm_budget=budget, count_policy="bitmap")
     alone = [A.wait(A.submit(r)) for r in reqs[:k]]
     A.close()
 
@@ -626,35 +746,32 @@ def run_serve(args):
                 r.count_sum, r.count_digest)
 
     same = all(key(a) == key(b) for a, b in zip(alone, res[:k]))
-    qlat = sorted(r.latency_ms for r in res if r.type == accx.REQ_QUERY)
-    qrun = sorted(r.run_ms for r in res if r.type == accx.REQ_QUERY)
-    pct = lambda v, p: round(v[min(len(v) - 1, int(round(p * (len(v) - 1))))], 3) if v else None
-    line = {"metric": "SCAN serving p50/p99 ms (continuous batching)", "value": round(st["query_p99_ms"], 3),
-            "unit": "ms", "n_gpus": world, "higher_is_better": False, "data": "synthetic",
-            "config": {"workload": "resident R-MAT scale %d ef 16 seed %d; Poisson %.1f req/s, %d requests, %.0f%% "
-                                   "new-graph counts (R-MAT scale 14-22), queries eps~U[0.1,0.9] mu~U{2..20}"
-                                   % (args.serve_scale, 1 + rank, args.serve_rate, len(reqs), 100 * args.count_frac),
-                       "n": G.n, "m": G.m, "workers": args.serve_workers, "hbm_budget_gb": args.serve_budget_gb,
-                       "resident_gen_s": round(gen_s, 2), "resident_count_s": round(count_s, 2)},
-            "query": {"p50_ms": st["query_p50_ms"], "p99_ms": st["query_p99_ms"], "run_p50_ms": pct(qrun, 0.5),
-                      "run_p99_ms": pct(qrun, 0.99), "n": len(qlat)},
-            "count": {"p50_ms": st["count_p50_ms"], "p99_ms": st["count_p99_ms"],
-                      "n": sum(1 for r in res if r.type == accx.REQ_COUNT)},
-            "throughput_rps": round(st["throughput_rps"], 2), "max_concurrent": st["max_concurrent"],
-            "peak_budget_gb": round(st["peak_bytes"] / (1 << 30), 2), "failed": st["failed"],
-            "same_alone_and_mixed": {"checked": k, "identical": bool(same)}}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    out = {"metric": "SCAN serving p50/p99 ms (continuous batching)",
+           "value": points["light"]["query"]["p99_ms"], "unit": "ms", "higher_is_better": False,
+           "workload": "resident R-MAT scale %d ef 16 seed 1; Poisson arrivals, %.0f%% new-graph counts (R-MAT "
+                       "scale 14-22), queries eps~U[0.1,0.9] mu~U{2..20}" % (args.serve_scale, 100 * args.count_frac),
+           "n": G.n, "m": G.m, "workers": args.serve_workers, "hbm_budget_gb": args.serve_budget_gb,
+           "resident_gen_s": round(gen_s, 2), "resident_count_s": round(count_s, 2),
+           "points": points, "same_alone_and_mixed": {"checked": k, "identical": bool(same)}}
+    G.free()
+    return out
 
 
 def main():
     args = parse()
-    if args.workload == "serve":
-        run_serve(args)
+    if args.workload in ("batch", "serve", "skew"):
+        import torch
+        from acctricnt_gb300 import sched
+        S, _ = sched.default_scheduler()
+        if args.workload == "batch":
+            r = run_batch(args, S, torch.cuda.Stream())
+        elif args.workload == "serve":
+            r = run_serve(args, S)
+        else:
+            r = run_skew(args, S, torch.cuda.Stream())
+        print(json.dumps(r), flush=True)
         return
-    if args.workload == "batch":
-        run_batch(args)
-    elif args.impl == "reference":
+    if args.impl == "reference":
         run_reference(args)
     else:
         run_gb300(args)

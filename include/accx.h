@@ -302,6 +302,71 @@ int accx_bucket_features_oriented(accx_graph *g, float *features);
 int accx_model_table_for_oriented(accx_model *m, accx_graph *g, uint8_t *table);
 int accx_graph_set_model_oriented(accx_graph *g, accx_model *m);
 
+/* ---- scheduler: training data, training, calibration, count plan, model file --
+ * Replaces the reference's fixed kernel choice: the backend linked into each
+ * CMake target (scan-query-cuda/CMakeLists.txt:114-117, each target defining its
+ * own SCAN_XP::CheckCore) and the ratio-50 rule inside it
+ * (scan_xp_multi_gpu_multi_pass_common.cu:57-59, :105-117), which stays the
+ * fallback when no model is available.  A scheduler holds two cost models, one
+ * for the direct kernels and one for the oriented kernels. */
+
+/* Per-bucket kernel timings of a graph, the models' training data: for every
+ * bucket with at least min_edges owned edges and every kind k, one count with
+ * only that bucket enabled under kind k (all others ACCX_KIND_SKIP), best of
+ * reps; ms[b*ACCX_NUM_KINDS + k] = its counting-phase time minus that of a count
+ * with every bucket skipped (NaN for buckets not timed).  edges[b] as
+ * accx_bucket_stats (accx_bucket_stats_oriented when orient = 1). */
+int accx_bucket_timings(accx_graph *g, int orient, int reps, uint64_t min_edges, uint64_t *edges, float *ms,
+                        void *stream);
+
+#define ACCX_SCHED_NOFFSETS 8   /* bitmap-kind offsets tried: 0, -0.5, -1, -1.5, -2, -3, -5, -64 */
+typedef struct accx_sched accx_sched;
+typedef struct {
+  uint64_t seed;  /* model initialisation (0 = 1) */
+  int epochs;     /* Adam epochs per model (0 = 4000; 800 when quick) */
+  float lr;       /* learning rate (0 = 3e-3) */
+  int reps;       /* timing repetitions per bucket and kind (0 = 2) */
+  int quick;      /* 1: four small training graphs, also used for calibration (tests) */
+} accx_sched_config;
+typedef struct {
+  uint32_t rows[2];                   /* training rows per model (0 direct, 1 oriented) */
+  float loss_initial[2], loss_final[2];
+  float bitmap_offset[2];             /* the calibrated log2 offset of the bitmap kind */
+  float calib_relative[2][ACCX_SCHED_NOFFSETS];  /* size-weighted relative count time per offset */
+  double collect_s[2], train_s[2], calibrate_s[2];
+  int quick;
+} accx_sched_info;
+typedef struct {
+  int orient;                 /* the chosen mode */
+  double predicted_ms[2];     /* each model's predicted time of its own table (direct, oriented) */
+  float calibrated_offset;    /* the chosen mode's bitmap offset before tuning */
+  float bitmap_offset;        /* ... and after */
+  int tuned;
+  float offsets[ACCX_SCHED_NOFFSETS];
+  float tune_ms[ACCX_SCHED_NOFFSETS];  /* whole-count time per candidate offset (tuned only) */
+  double tune_s;
+} accx_sched_plan;
+
+/* Trains both models on the device: per-bucket timings of seven seeded graphs
+ * (relabeled), Adam training with the library's kernels, then the bitmap
+ * offset calibrated on whole counts of those graphs plus R-MAT 20 and 22.
+ * Takes tens of seconds on a GB300 (a few with quick = 1).  cfg NULL = defaults. */
+int accx_sched_train(const accx_sched_config *cfg, accx_sched **out);
+int accx_sched_free(accx_sched *s);
+/* A text file of both models (parameters, kind offsets, training record). */
+int accx_sched_save(const accx_sched *s, const char *path);
+int accx_sched_load(const char *path, accx_sched **out);
+int accx_sched_get_info(const accx_sched *s, accx_sched_info *info);
+/* The scheduler's model for a mode (owned by the scheduler). */
+int accx_sched_model(accx_sched *s, int orient, accx_model **out);
+/* Plans the counts of g: attaches both models (ACCX_POLICY_MODEL), predicts each
+ * mode's time from its own per-bucket table and picks the faster mode.  tune = 1
+ * also times one whole count per bitmap offset on g and keeps the fastest in the
+ * chosen model (it then applies to every graph that model serves).  opts
+ * (optional) is filled for accx_cn_count: policy ACCX_POLICY_MODEL, orient. */
+int accx_sched_plan_for(accx_sched *s, accx_graph *g, int tune, accx_count_opts *opts, accx_sched_plan *plan,
+                        void *stream);
+
 /* ---- batches of uneven graphs -------------------------------------------------
  * No reference counterpart (the reference counts one graph per process).  A
  * batch joins K graphs into one disjoint-union CSR on the device; one count and

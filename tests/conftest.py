@@ -34,3 +34,23 @@ def has_gpu():
         return torch.cuda.is_available()
     except Exception:
         return False
+
+
+@pytest.fixture(scope="session")
+def quick_sched_file(tmp_path_factory):
+    """A scheduler file trained on this GPU in quick mode by the library's own
+    training CLI (accx-sched-train)."""
+    import subprocess
+    from acctricnt_gb300 import BUILD_DIR
+    path = str(tmp_path_factory.mktemp("sched") / "quick.model")
+    r = subprocess.run([os.path.join(BUILD_DIR, "accx-sched-train"), path, "quick"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return path
+
+
+@pytest.fixture(scope="session")
+def default_sched():
+    """The full scheduler of the build folder (trained on this GPU when absent)."""
+    from acctricnt_gb300 import sched
+    s, _ = sched.default_scheduler()
+    return s

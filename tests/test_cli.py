@@ -22,26 +22,36 @@ def test_cli_usage_and_missing_graph(tmp_path):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", golden_cases())
-@pytest.mark.parametrize("variant", ["plain", "varying", "heuristic_norelabel", "direct"])
-def test_cli_result_file_matches_reference(name, variant, tmp_path):
+@pytest.mark.parametrize("variant", ["model", "fallback", "varying", "heuristic_norelabel", "oriented_bitmap"])
+def test_cli_result_file_matches_reference(name, variant, tmp_path, quick_sched_file):
+    """With a scheduler file (the learned plan) and without one (the reference's
+    ratio-50 rule), and under explicit policies: the same result file, byte for
+    byte the reference's."""
     g = load_golden(name)
     d = str(tmp_path)
     accx.write_graph_dir(d, g["off"], g["dst"])
     eps, mu = repr(float(g["eps"])), str(int(g["mu"]))
-    env = dict(os.environ)
+    env = dict(os.environ, ACCX_SCHED_MODEL=quick_sched_file)
     if variant == "varying":
         cmd = [CLI_VAR, d, eps, mu, "4", "1", "8", os.path.join(d, "log.txt")]
     else:
         cmd = [CLI, d, eps, mu, "4", os.path.join(d, "log.txt")]
+    if variant == "fallback":
+        env.update(ACCX_SCHED_MODEL=os.path.join(d, "no-such.model"))
     if variant == "heuristic_norelabel":
         env.update(ACCX_POLICY="heuristic", ACCX_RELABEL="0")
-    if variant == "direct":  # the reference's formulation: full-list intersections
-        env.update(ACCX_ORIENT="0")
+    if variant == "oriented_bitmap":
+        env.update(ACCX_POLICY="bitmap", ACCX_ORIENT="1")
     r = subprocess.run(cmd, capture_output=True, text=True, env=env)
     assert r.returncode == 0, r.stderr
     with open(os.path.join(d, str(g["result_name"])), "rb") as f:
         assert f.read() == g["result"].tobytes()
-    assert "Step1 - CheckCore" in open(os.path.join(d, "log.txt")).read()
+    log = open(os.path.join(d, "log.txt")).read()
+    assert "Step1 - CheckCore" in log
+    if variant in ("model", "varying"):
+        assert "kernel plan: learned scheduler" in log
+    if variant == "fallback":
+        assert "kernel plan: reference ratio-50 rule" in log
 
 
 def _np_convert(text):

@@ -128,32 +128,6 @@ def test_oriented_model_table_is_argmin_and_counts_are_exact():
     assert np.array_equal(G.count(policy="model", orient=True), ref)
 
 
-def test_learned_oriented_schedule_on_an_unseen_graph():
-    from acctricnt_gb300 import sched
-    model, info = sched.train_default(epochs=2000, orient=True)
-    assert info["loss_final"] < info["loss_initial"]
-    G = accx.Graph.generate(accx.rmat_params(19, 16, seed=99))
-    G.relabel()
-    edges, T = sched.bucket_timings(G, reps=2, orient=True)
-    e, so, sp = G.bucket_stats(orient=True)
-    heur = sched.heuristic_table(e, so, sp)
-    # the network itself learned the per-bucket costs it was trained on (buckets
-    # timed alone): its raw choice is near the per-bucket best and beats the rule
-    bias = model.kind_bias()
-    model.set_kind_bias([0.0, 0.0, 0.0])
-    raw = model.table_for(G, orient=True)
-    assert sched.table_time(raw, T) < sched.table_time(heur, T)
-    assert sched.regret(raw, edges, T)["regret_frac"] < 0.5
-    # with the offset fitted on whole counts, its table beats the rule as a whole count
-    model.set_kind_bias(bias)
-    t_model = sched._count_phase_ms(G, model.table_for(G, orient=True).reshape(-1), 3, None, True)
-    t_heur = sched._count_phase_ms(G, heur.reshape(-1), 3, None, True)
-    assert t_model < t_heur
-    direct, _ = sched.train_default(epochs=500)
-    pl = sched.plan(G, direct, model)
-    assert set(pl["predicted_ms"]) == {"direct", "oriented"} and pl["predicted_ms"]["oriented"] > 0
-
-
 def test_kind_bias_steers_the_table():
     m = accx.Model(seed=8)
     G = accx.Graph.generate(accx.rmat_params(14, 16, seed=5))
@@ -171,17 +145,3 @@ def test_kind_bias_steers_the_table():
     assert np.array_equal(G.count(policy="model", orient=True), ref)
     with pytest.raises(accx.AccxError):
         m.set_kind_bias([0.0, float("nan"), 0.0])
-
-
-def test_tune_offset_keeps_a_candidate_and_counts_stay_exact():
-    from acctricnt_gb300 import sched
-    m = accx.Model(seed=9)
-    G = accx.Graph.generate(accx.rmat_params(15, 16, seed=6))
-    ref = G.count(policy="heuristic")
-    G.relabel()
-    info = sched.tune_offset(G, m, orient=True, reps=1)
-    assert len(info["candidate_ms"]) == len(sched.BITMAP_OFFSETS)
-    assert info["kind_bias"][2] in sched.BITMAP_OFFSETS
-    assert np.isclose(m.kind_bias()[2], info["kind_bias"][2])
-    G.set_model(m, orient=True)
-    assert np.array_equal(G.count(policy="model", orient=True), ref)

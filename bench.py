@@ -54,7 +54,9 @@ def parse():
     ap.add_argument("--serve-scale", type=int, default=26)
     ap.add_argument("--serve-rate", type=float, default=10.0)
     ap.add_argument("--serve-requests", type=int, default=200)
-    ap.add_argument("--serve-rate-high", type=float, default=400.0)
+    ap.add_argument("--serve-rate-high", type=float, default=100.0,
+                    help="the second load point: near the server's capacity (about 150 requests/s at R-MAT 26), "
+                         "where every worker is busy but the queue stays short")
     ap.add_argument("--serve-requests-high", type=int, default=400)
     ap.add_argument("--serve-workers", type=int, default=4)
     ap.add_argument("--serve-budget-gb", type=float, default=64.0)

@@ -88,3 +88,24 @@ def test_oriented_capture_and_autotune_match_eager():
         B.launch(stream=s.cuda_stream)
         s.synchronize()
         assert np.array_equal(U.read_counts(), want)
+
+
+def test_bench_batch_against_the_oracle(default_sched):
+    """The batch workload exactly as the bench runs it -- 512 graphs, undirected
+    edge draws log-uniform 1K-2M, R-MAT scale 10-18 / ER mix, seed 1 -- counted
+    as one captured oriented launch under the scheduler's model: every graph's
+    slice of the union counts equals the oracle's CheckCoreBitmap on that graph."""
+    import torch
+    from oracle import oracle
+    gs = [accx.Graph.generate(p) for p in workloads.batch_uneven(k=512, seed=1)]
+    B = accx.Batch(gs)
+    U = B.union
+    U.relabel()
+    U.set_model(default_sched.model(True), orient=True)
+    s = torch.cuda.Stream()
+    B.capture(policy="model", bias=2, stream=s.cuda_stream, orient=True)
+    B.launch(stream=s.cuda_stream)
+    s.synchronize()
+    for i, (G, c) in enumerate(zip(gs, B.split(U.read_counts()))):
+        off, dst = G.download()
+        assert np.array_equal(c, oracle.cn_count(off, dst, nthreads=0)), i

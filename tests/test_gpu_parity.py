@@ -118,6 +118,32 @@ def test_chung_lu_skew_parity_with_oracle():
         assert np.array_equal(G.count(policy=pol, bias=2), ref), pol
 
 
+@pytest.mark.parametrize("kind", ["chung_lu", "erdos_renyi"])
+def test_skew_config_scaled_down_parity_with_oracle(kind, default_sched):
+    """The learned-scheduler skew config scaled down by 10: Chung-Lu with 2M
+    vertices, exponent 2.1, mean degree 24, max expected degree 100K (the
+    20M-vertex config's max-degree/n ratio), and Erdos-Renyi with 2M vertices,
+    mean degree 24.  The scheduler's plan and every fixed policy in both modes
+    equal the oracle's CheckCoreBitmap entry for entry."""
+    if kind == "chung_lu":
+        p = accx.chung_lu_params(2_000_000, 24, 2.1, 1e5, seed=1)
+    else:
+        p = accx.er_params(2_000_000, 24, seed=1)
+    G = accx.Graph.generate(p)
+    off, dst = G.download()
+    ref = oracle.cn_count(off, dst, nthreads=0)
+    assert np.array_equal(G.count(policy="heuristic", bias=2), ref)
+    G.relabel()
+    pl = default_sched.plan(G)
+    assert np.array_equal(G.count(policy="model", orient=pl["orient"], bias=2), ref)
+    for pol in ("gallop", "bitmap"):
+        assert np.array_equal(G.count(policy=pol, bias=2), ref), pol
+    for pol in ("merge", "gallop", "bitmap"):
+        assert np.array_equal(G.count(policy=pol, bias=2, orient=True), ref), pol
+    if kind == "chung_lu":
+        assert np.diff(off.astype(np.int64)).max() > 20_000  # the heavy head is there
+
+
 def test_large_rmat_policies_agree_and_are_symmetric():
     """Size-independent properties at R-MAT scale 20: all policies agree, the
     count array is symmetric (cnt[e] == cnt[reverse(e)]), and sampled entries

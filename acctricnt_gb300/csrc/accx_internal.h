@@ -135,6 +135,9 @@ int accx_prefix_lengths(accx_graph *g, cudaStream_t s);
 void accx_model_release(accx_graph *g);
 int accx_model_table(accx_graph *g, uint8_t *table);
 int accx_model_table_device(accx_graph *g, cudaStream_t s, int orient);
+// Predicted time (ms) of a model's own table on a graph's buckets (direct: mode 0,
+// oriented: mode 1), computed on the device.
+int accx_model_plan_ms(accx_model *m, accx_graph *g, int mode, cudaStream_t s, double *ms);
 
 // Exclusive/inclusive helpers implemented in gen.cu.
 // Row index of every 256-entry tile of a CSR (graph.cu), allocated on g's home stream.

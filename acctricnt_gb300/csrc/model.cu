@@ -145,11 +145,14 @@ __global__ void k_model_adam(float *__restrict__ master, __half *__restrict__ w,
 // launch; a row's first layer is per lane, the second gathers the 32 first-layer
 // activations by shuffles, the output layer is a warp sum.  With `table` set the
 // rows are a graph's bucket features and the argmin kind of every populated
-// bucket is written to table[row]; otherwise the outputs go to y.
+// bucket is written to table[row] (and, with `cost` set, the bucket's predicted
+// time in seconds, edges x 2^(the chosen kind's output), to cost[row]); otherwise
+// the outputs go to y.
 __global__ void __launch_bounds__(256) k_model_infer(const __half *__restrict__ w, const float *__restrict__ x,
                                                      uint32_t k, float *__restrict__ y,
                                                      const unsigned long long *__restrict__ edges,
-                                                     uint8_t *__restrict__ table, accx_kind_bias kb) {
+                                                     uint8_t *__restrict__ table, accx_kind_bias kb,
+                                                     double *__restrict__ cost = nullptr) {
   const int lane = threadIdx.x & 31;
   float w1[IN], w2[H], w3[OUT], b3[OUT];
 #pragma unroll
@@ -188,6 +191,7 @@ __global__ void __launch_bounds__(256) k_model_infer(const __half *__restrict__ 
         for (int o = 1; o < OUT; o++)
           if (out[o] + kb.b[o] < out[best] + kb.b[best]) best = o;
         table[r] = (edges && edges[r] == 0) ? (uint8_t)ACCX_KIND_MERGE : (uint8_t)best;
+        if (cost) cost[r] = (edges && edges[r]) ? (double)edges[r] * exp2((double)out[best]) : 0.0;
       } else {
 #pragma unroll
         for (int o = 0; o < OUT; o++) y[(size_t)r * OUT + o] = out[o];
@@ -280,6 +284,9 @@ struct accx_graph_model_state {
   bool ready[2] = {false, false};
   const uint32_t *csr[2] = {nullptr, nullptr};
   accx_model *model[2] = {nullptr, nullptr};
+  // plan costs (accx_model_plan_ms): a scratch table, per-bucket costs and their sum
+  uint8_t *d_ptable = nullptr;
+  double *d_cost = nullptr;  // NBB + 1
 };
 
 static accx_graph_model_state *state_of(accx_graph *g) {
@@ -294,6 +301,8 @@ void accx_model_release(accx_graph *g) {
       if (st->d_stats[i]) cudaFree(st->d_stats[i]);
       if (st->d_feat[i]) cudaFree(st->d_feat[i]);
     }
+    if (st->d_ptable) cudaFree(st->d_ptable);
+    if (st->d_cost) cudaFree(st->d_cost);
     delete st;
   }
   g->model = nullptr;
@@ -338,6 +347,43 @@ int accx_model_table_device(accx_graph *g, cudaStream_t s, int orient) {
   k_model_infer<<<8, 256, 0, s>>>(st->model[mode]->d_w, st->d_feat[mode], NBB, nullptr, st->d_stats[mode], g->d_table,
                                   kb);
   ACCX_CUDA_TRY(cudaGetLastError());
+  return ACCX_OK;
+}
+
+// One block sums the per-bucket costs in a fixed order (the same total on every run).
+__global__ void __launch_bounds__(256) k_sum_cost(const double *__restrict__ cost, int k, double *__restrict__ out) {
+  __shared__ double part[256];
+  double a = 0;
+  for (int i = threadIdx.x; i < k; i += 256) a += cost[i];
+  part[threadIdx.x] = a;
+  __syncthreads();
+  for (int d = 128; d >= 1; d >>= 1) {
+    if ((int)threadIdx.x < d) part[threadIdx.x] += part[threadIdx.x + d];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = part[0];
+}
+
+// Predicted time (ms) of model m's own per-bucket table on g's buckets of the
+// given mode: the sum over populated buckets of edges x 2^(the chosen kind's
+// prediction).  The buffers live with the graph; one 8-byte copy comes back.
+int accx_model_plan_ms(accx_model *m, accx_graph *g, int mode, cudaStream_t s, double *ms) {
+  if (!m || !g || !ms || (mode != 0 && mode != 1)) return ACCX_ERR_INVALID_ARG;
+  accx_graph_model_state *st = state_of(g);
+  if (!st) return ACCX_ERR_OOM;
+  int rc = ensure_features(g, s, mode);
+  if (rc) return rc;
+  if (!st->d_ptable) ACCX_CUDA_TRY(cudaMalloc(&st->d_ptable, NBB));
+  if (!st->d_cost) ACCX_CUDA_TRY(cudaMalloc(&st->d_cost, sizeof(double) * (NBB + 1)));
+  accx_kind_bias kb;
+  for (int o = 0; o < OUT; o++) kb.b[o] = m->bias[o];
+  k_model_infer<<<8, 256, 0, s>>>(m->d_w, st->d_feat[mode], NBB, nullptr, st->d_stats[mode], st->d_ptable, kb,
+                                  st->d_cost);
+  k_sum_cost<<<1, 256, 0, s>>>(st->d_cost, NBB, st->d_cost + NBB);
+  double sec = 0;
+  ACCX_CUDA_TRY(cudaMemcpyAsync(&sec, st->d_cost + NBB, sizeof(double), cudaMemcpyDeviceToHost, s));
+  ACCX_CUDA_TRY(cudaStreamSynchronize(s));
+  *ms = sec * 1e3;
   return ACCX_OK;
 }
 

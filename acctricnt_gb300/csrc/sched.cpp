@@ -366,36 +366,6 @@ extern "C" int accx_sched_load(const char *path, accx_sched **out) {
   return ACCX_OK;
 }
 
-// Predicted time (ms) of a model's own table on g: sum over populated buckets of
-// edges x 2^(predicted log2 s/edge of the chosen kind).
-static int predicted_ms(accx_model *m, accx_graph *g, int orient, double *out) {
-  std::vector<uint64_t> e(NBK);
-  std::vector<double> so(NBK), sp(NBK);
-  std::vector<float> X(NBK * ACCX_MODEL_IN);
-  uint8_t t[NBK];
-  int rc = orient ? accx_bucket_stats_oriented(g, e.data(), so.data(), sp.data())
-                  : accx_bucket_stats(g, e.data(), so.data(), sp.data());
-  if (!rc) rc = orient ? accx_bucket_features_oriented(g, X.data()) : accx_bucket_features(g, X.data());
-  if (!rc) rc = model_table(m, g, orient, t);
-  if (rc) return rc;
-  std::vector<float> xs;
-  std::vector<int> bs;
-  for (int b = 0; b < NBK; b++)
-    if (e[b] > 0) {
-      xs.insert(xs.end(), X.begin() + (size_t)b * ACCX_MODEL_IN, X.begin() + (size_t)(b + 1) * ACCX_MODEL_IN);
-      bs.push_back(b);
-    }
-  *out = 0;
-  if (bs.empty()) return ACCX_OK;
-  std::vector<float> y(bs.size() * ACCX_MODEL_OUT);
-  rc = accx_model_predict(m, xs.data(), (uint32_t)bs.size(), y.data());
-  if (rc) return rc;
-  double tot = 0;
-  for (size_t i = 0; i < bs.size(); i++) tot += (double)e[bs[i]] * exp2((double)y[i * ACCX_MODEL_OUT + t[bs[i]]]);
-  *out = tot * 1e3;
-  return ACCX_OK;
-}
-
 extern "C" int accx_sched_plan_for(accx_sched *s, accx_graph *g, int tune, accx_count_opts *opts,
                                    accx_sched_plan *plan, void *stream) {
   if (!s || !g || !s->model[0] || !s->model[1]) return ACCX_ERR_INVALID_ARG;
@@ -403,8 +373,8 @@ extern "C" int accx_sched_plan_for(accx_sched *s, accx_graph *g, int tune, accx_
   memset(&pl, 0, sizeof(pl));
   int rc = accx_graph_set_model(g, s->model[0]);
   if (!rc) rc = accx_graph_set_model_oriented(g, s->model[1]);
-  if (!rc) rc = predicted_ms(s->model[0], g, 0, &pl.predicted_ms[0]);
-  if (!rc) rc = predicted_ms(s->model[1], g, 1, &pl.predicted_ms[1]);
+  if (!rc) rc = accx_model_plan_ms(s->model[0], g, 0, (cudaStream_t)stream, &pl.predicted_ms[0]);
+  if (!rc) rc = accx_model_plan_ms(s->model[1], g, 1, (cudaStream_t)stream, &pl.predicted_ms[1]);
   if (rc) return rc;
   pl.orient = pl.predicted_ms[1] < pl.predicted_ms[0] ? 1 : 0;
   accx_model *m = s->model[pl.orient];

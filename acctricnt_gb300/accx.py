@@ -106,7 +106,7 @@ class SchedInfo(C.Structure):
 class SchedPlan(C.Structure):
     _fields_ = [("orient", C.c_int), ("predicted_ms", C.c_double * 2), ("calibrated_offset", C.c_float),
                 ("bitmap_offset", C.c_float), ("tuned", C.c_int), ("offsets", C.c_float * SCHED_NOFFSETS),
-                ("tune_ms", C.c_float * SCHED_NOFFSETS), ("tune_s", C.c_double)]
+                ("tune_ms", C.c_float * SCHED_NOFFSETS), ("tune_s", C.c_double), ("mode_ms", C.c_double * 2)]
 
 
 def _load():
@@ -673,6 +673,7 @@ class Scheduler:
              "predicted_ms": {"direct": round(p.predicted_ms[0], 3), "oriented": round(p.predicted_ms[1], 3)},
              "calibrated_offset": float(p.calibrated_offset), "bitmap_offset": float(p.bitmap_offset)}
         if p.tuned:
+            d["mode_ms"] = {"direct": round(p.mode_ms[0], 3), "oriented": round(p.mode_ms[1], 3)}
             d["tune"] = {"offsets": [float(x) for x in p.offsets], "candidate_ms": [round(float(x), 3) for x in p.tune_ms],
                          "seconds": round(p.tune_s, 2)}
         return d

@@ -104,9 +104,19 @@ bool accx_is_device_ptr(const void *p) {
 // that mapping at link speed, where the copy engines were measured several
 // times slower into device blocks that had been freed and reused.  Pageable
 // host memory and unaligned ends go through cudaMemcpyAsync.
+// Each thread keeps four 16-byte loads in flight (each warp still reads 512
+// contiguous bytes per load): the host link's latency is long.
 __global__ void k_copy16(uint4 *__restrict__ d, const uint4 *__restrict__ s, size_t n16) {
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += (size_t)gridDim.x * blockDim.x)
-    d[i] = s[i];
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + 3 * stride < n16; i += 4 * stride) {
+    const uint4 a = s[i], b = s[i + stride], c = s[i + 2 * stride], e = s[i + 3 * stride];
+    d[i] = a;
+    d[i + stride] = b;
+    d[i + 2 * stride] = c;
+    d[i + 3 * stride] = e;
+  }
+  for (; i < n16; i += stride) d[i] = s[i];
 }
 
 // The device-side address of pinned (mapped) host memory, or nullptr.

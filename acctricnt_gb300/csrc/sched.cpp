@@ -92,9 +92,10 @@ static std::vector<accx_gen_params> calibration_graphs(int quick) {
   return g;
 }
 
-// Counting-phase time (merge + gallop + bitmap, ms) of one count with `table`,
-// best of reps.
-static int table_count_ms(accx_graph *g, const uint8_t *table, int orient, int reps, cudaStream_t s, double *ms) {
+// Counting-phase time (merge + gallop + bitmap, ms; with `whole`, every phase of
+// the count) of one count with `table`, best of reps.
+static int table_count_ms(accx_graph *g, const uint8_t *table, int orient, int reps, cudaStream_t s, double *ms,
+                          bool whole = false) {
   accx_count_opts o;
   memset(&o, 0, sizeof(o));
   o.policy = ACCX_POLICY_TABLE;
@@ -108,7 +109,8 @@ static int table_count_ms(accx_graph *g, const uint8_t *table, int orient, int r
     float ph[ACCX_NUM_PHASES];
     rc = accx_cn_last_timings(g, ph);
     if (rc) return rc;
-    const double t = (double)ph[ACCX_PHASE_MERGE] + ph[ACCX_PHASE_GALLOP] + ph[ACCX_PHASE_BITMAP];
+    double t = (double)ph[ACCX_PHASE_MERGE] + ph[ACCX_PHASE_GALLOP] + ph[ACCX_PHASE_BITMAP];
+    if (whole) t += (double)ph[ACCX_PHASE_PLAN] + ph[ACCX_PHASE_MIRROR];
     if (best < 0 || t < best) best = t;
   }
   *ms = best;
@@ -377,6 +379,21 @@ extern "C" int accx_sched_plan_for(accx_sched *s, accx_graph *g, int tune, accx_
   if (!rc) rc = accx_model_plan_ms(s->model[1], g, 1, (cudaStream_t)stream, &pl.predicted_ms[1]);
   if (rc) return rc;
   pl.orient = pl.predicted_ms[1] < pl.predicted_ms[0] ? 1 : 0;
+  auto t0 = clk::now();
+  if (tune) {
+    // the mode by measurement: each mode's own table as a whole count (every
+    // phase), best of two; the predictions extrapolate poorly to graphs far from
+    // the training set (an Erdos-Renyi graph 150x the training one)
+    for (int o = 0; o < 2; o++) {
+      uint8_t t[NBK];
+      double ms = 0;
+      rc = model_table(s->model[o], g, o, t);
+      if (!rc) rc = table_count_ms(g, t, o, 2, (cudaStream_t)stream, &ms, true);
+      if (rc) return rc;
+      pl.mode_ms[o] = ms;
+    }
+    pl.orient = pl.mode_ms[1] < pl.mode_ms[0] ? 1 : 0;
+  }
   accx_model *m = s->model[pl.orient];
   float b[ACCX_MODEL_OUT];
   rc = accx_model_get_kind_bias(m, b);
@@ -385,7 +402,6 @@ extern "C" int accx_sched_plan_for(accx_sched *s, accx_graph *g, int tune, accx_
   pl.calibrated_offset = b[2];
   if (tune) {
     // one whole count per candidate offset on this graph; ties keep the offset in use
-    auto t0 = clk::now();
     int bi = -1;
     double best = 0;
     for (int c = 0; c < ACCX_SCHED_NOFFSETS; c++) {

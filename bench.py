@@ -222,7 +222,26 @@ def measure_e2e(G, policy, reps, sched=None, orient=False):
     t_dst = torch.from_numpy(dst).pin_memory()
     t_cnt = torch.empty(G.m, dtype=torch.int32).pin_memory()
     times, modes = [], set()
-    for i in range(reps + 1):
+    stages = {}
+    for i in range(reps + 2):
+        if i == reps + 1:  # one more, untimed, with a synchronisation after each stage
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            H = accx.Graph.from_device(t_off.data_ptr(), t_dst.data_ptr(), G.n, G.m, validate=True)
+            torch.cuda.synchronize()
+            stages["upload_validate"] = time.perf_counter() - t0
+            H.relabel()
+            torch.cuda.synchronize()
+            stages["relabel"] = time.perf_counter() - t0 - sum(stages.values())
+            pl = sched.plan(H) if sched is not None else {"policy": policy, "orient": orient}
+            stages["plan"] = time.perf_counter() - t0 - sum(stages.values())
+            H.count(policy=pl["policy"], out=None, orient=pl["orient"])
+            torch.cuda.synchronize()
+            stages["first_count"] = time.perf_counter() - t0 - sum(stages.values())
+            H.count(policy=pl["policy"], out=t_cnt.data_ptr(), orient=pl["orient"])
+            stages["count_and_download"] = time.perf_counter() - t0 - sum(stages.values())
+            H.free()
+            break
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         H = accx.Graph.from_device(t_off.data_ptr(), t_dst.data_ptr(), G.n, G.m, validate=True)
@@ -240,6 +259,7 @@ def measure_e2e(G, policy, reps, sched=None, orient=False):
     t = statistics.median(times)
     return {"value": round(G.m / t / 1e9, 4), "unit": UNIT, "h2d_bytes_per_step": 4 * (G.n + 1) + 4 * G.m,
             "d2h_bytes_per_step": 4 * G.m, "ms_per_step": round(t * 1e3, 3), "reps": reps,
+            "stages_ms_one_run": {k: round(v * 1e3, 2) for k, v in stages.items()},
             "ms_all": [round(x * 1e3, 3) for x in times],
             "path": "accx_graph_create(host pinned CSR, validate) + accx_graph_relabel + %saccx_cn_count(%s policy, "
                     "%s, host pinned out)" % ("accx_sched_plan_for + " if sched is not None else "", policy,

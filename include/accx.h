@@ -345,6 +345,7 @@ typedef struct {
   float offsets[ACCX_SCHED_NOFFSETS];
   float tune_ms[ACCX_SCHED_NOFFSETS];  /* whole-count time per candidate offset (tuned only) */
   double tune_s;
+  double mode_ms[2];          /* tuned only: each mode's own table as a whole count (direct, oriented) */
 } accx_sched_plan;
 
 /* Trains both models on the device: per-bucket timings of seven seeded graphs
@@ -361,7 +362,8 @@ int accx_sched_get_info(const accx_sched *s, accx_sched_info *info);
 int accx_sched_model(accx_sched *s, int orient, accx_model **out);
 /* Plans the counts of g: attaches both models (ACCX_POLICY_MODEL), predicts each
  * mode's time from its own per-bucket table and picks the faster mode.  tune = 1
- * also times one whole count per bitmap offset on g and keeps the fastest in the
+ * instead picks the mode by measurement (each mode's table as a whole count),
+ * then times one whole count per bitmap offset on g and keeps the fastest in the
  * chosen model (it then applies to every graph that model serves).  opts
  * (optional) is filled for accx_cn_count: policy ACCX_POLICY_MODEL, orient. */
 int accx_sched_plan_for(accx_sched *s, accx_graph *g, int tune, accx_count_opts *opts, accx_sched_plan *plan,

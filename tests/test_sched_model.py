@@ -115,6 +115,8 @@ def test_plan_tuning_keeps_a_candidate_and_counts_stay_exact(quick_sched_file):
     assert len(pl["tune"]["candidate_ms"]) == len(pl["tune"]["offsets"]) == accx.SCHED_NOFFSETS
     assert pl["bitmap_offset"] in pl["tune"]["offsets"]
     assert np.isclose(S.model(pl["orient"]).kind_bias()[2], pl["bitmap_offset"])
+    # a tuned plan picks the mode by measurement
+    assert pl["orient"] == (pl["mode_ms"]["oriented"] < pl["mode_ms"]["direct"])
     assert np.array_equal(G.count(policy="model", orient=pl["orient"]), ref)
 
 

@@ -161,14 +161,6 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32) k_gallop_or(const uint32_t *
   if (gl == 0 && found) atomicAdd(&ctr[C_MATCH + ACCX_KIND_GALLOP], found);
 }
 
-// Bit id mod 32 of a bitmap word (a wrap-mode funnel shift takes the shift
-// amount mod 32), and the number of set bits below it (a clamped funnel shift of
-// the word by 32 - (id mod 32) keeps exactly those bits; 32 gives 0).
-__device__ __forceinline__ bool or_bit(uint32_t wd, uint32_t id) { return __funnelshift_r(wd, wd, id) & 1u; }
-__device__ __forceinline__ uint32_t or_below(uint32_t wd, uint32_t id) {
-  return __popc(__funnelshift_lc(0u, wd, 32u - (id & 31u)));
-}
-
 // items[i] = the owner of bitmap work item i (items of one owner are contiguous).
 __global__ void k_item_fill(const unsigned long long *__restrict__ icnt, const unsigned long long *__restrict__ prefix,
                             uint32_t n, uint32_t cap, uint32_t *__restrict__ items) {
@@ -205,8 +197,8 @@ __device__ __forceinline__ uint32_t or_piece(const int32_t *__restrict__ dst, ui
     if (64u * (uint32_t)(r >> 1) >= rem) break;
     const uint32_t id = min((uint32_t)((r & 1) ? v[r >> 1].y : v[r >> 1].x), W);  // W: the zero word
     const uint32_t wd = words[id >> 5];
-    if (or_bit(wd, id)) {
-      const uint32_t rk = wbase[id >> 5] + or_below(wd, id);
+    if ((wd >> (id & 31u)) & 1u) {
+      const uint32_t rk = wbase[id >> 5] + __popc(wd & ((1u << (id & 31u)) - 1u));
       h++;
       atomicAdd(cl + 64u * (r >> 1) + (uint32_t)(r & 1), 1);
       if (rk < pxs) atomicAdd(&ocnt[rk], 1u);  // always true on a sorted CSR
@@ -383,8 +375,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bitmap_or(const uint32_t *__r
             // ids >= W (the -1 of lanes past the end) read the zero word
             const uint32_t id = min((uint32_t)xs[r], W);
             const uint32_t wd = words[id >> 5];
-            if (or_bit(wd, id)) {
-              const uint32_t rk = wbase[id >> 5] + or_below(wd, id);
+            if ((wd >> (id & 31u)) & 1u) {
+              const uint32_t rk = wbase[id >> 5] + __popc(wd & ((1u << (id & 31u)) - 1u));
               atomicAdd(cnt + gi[r], 1);
               if (rk < pxs) atomicAdd(&ocnt[rk], 1u);  // always true on a sorted CSR
               atomicAdd(&s_hit[sg[r]], 1u);

@@ -178,8 +178,10 @@ extern "C" int accx_autotune(accx_graph *g, const accx_count_opts *base, int rep
   if (!g || !best || reps < 1) return ACCX_ERR_INVALID_ARG;
   static const int cands_direct[][3] = {  // block warps, dense KiB, sparse KiB
       {32, 128, 64}, {32, 160, 32}, {32, 96, 96}, {32, 64, 64}, {16, 128, 64}, {16, 48, 32}, {24, 128, 64}};
-  static const int cands_orient[][3] = {  // block warps, dense KiB, owner-counter KiB
-      {16, 56, 8}, {16, 48, 16}, {16, 40, 16}, {16, 32, 16}, {32, 64, 16}, {32, 80, 16}, {16, 48, 8}};
+  // block warps, dense KiB, owner-counter KiB; {0, 0, 0} = the library's default
+  // shape, which splits the bitmap kind into a small-CTA and a full-window launch
+  static const int cands_orient[][3] = {
+      {16, 56, 8}, {16, 48, 16}, {16, 40, 16}, {16, 32, 16}, {32, 64, 16}, {32, 80, 16}, {0, 0, 0}};
   const bool orient = base && base->orient;
   const int(*cands)[3] = orient ? cands_orient : cands_direct;
   const int nc = 7;

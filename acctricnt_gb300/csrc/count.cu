@@ -641,11 +641,15 @@ static int g_sparse_kb = 64;
 static int g_or_dense_kb = 56;     // with 512-thread blocks two CTAs share an SM
 static int g_or_counter_kb = 8;
 static int g_or_block_warps = 16;
+// The first (small-CTA) launch of the oriented bitmap kind: its window (KiB) and
+// CTA size.  R-MAT 24 bitmap phase by (window, CTA size): 12-24 KiB at 256
+// threads 81.2-81.7 ms (four CTAs per SM), 32 KiB 95.4 ms (three per SM), 16 and
+// 24 KiB at 128 threads 93.5 and 127.4 ms; one 512-thread launch 82.9 ms.
 #ifndef OR_SMALL_KB
-#define OR_SMALL_KB 24u                // window of the first (small-CTA) oriented bitmap launch, KiB
+#define OR_SMALL_KB 24u
 #endif
 #ifndef OR_SMALL_NT
-#define OR_SMALL_NT 256                // its CTA size
+#define OR_SMALL_NT 256
 #endif
 #define OR_SMALL_W (OR_SMALL_KB * 8192u)
 

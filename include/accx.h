@@ -308,7 +308,8 @@ int accx_graph_set_model_oriented(accx_graph *g, accx_model *m);
  * own SCAN_XP::CheckCore) and the ratio-50 rule inside it
  * (scan_xp_multi_gpu_multi_pass_common.cu:57-59, :105-117), which stays the
  * fallback when no model is available.  A scheduler holds two cost models, one
- * for the direct kernels and one for the oriented kernels. */
+ * for the direct kernels and one for the oriented kernels.  It is not
+ * thread-safe: a tuned plan changes its models' bitmap offsets. */
 
 /* Per-bucket kernel timings of a graph, the models' training data: for every
  * bucket with at least min_edges owned edges and every kind k, one count with

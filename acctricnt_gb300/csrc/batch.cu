@@ -179,7 +179,7 @@ extern "C" int accx_autotune(accx_graph *g, const accx_count_opts *base, int rep
   static const int cands_direct[][3] = {  // block warps, dense KiB, sparse KiB
       {32, 128, 64}, {32, 160, 32}, {32, 96, 96}, {32, 64, 64}, {16, 128, 64}, {16, 48, 32}, {24, 128, 64}};
   // block warps, dense KiB, owner-counter KiB; {0, 0, 0} = the library's default
-  // shape, which splits the bitmap kind into a small-CTA and a full-window launch
+  // shape (256-thread CTAs, a 24 KiB window)
   static const int cands_orient[][3] = {
       {16, 56, 8}, {16, 48, 16}, {16, 40, 16}, {16, 32, 16}, {32, 64, 16}, {32, 80, 16}, {0, 0, 0}};
   const bool orient = base && base->orient;

@@ -36,8 +36,7 @@
 #define C_OWNER 9  // + kind: owner-side elements
 #define C_MATCH 12 // + kind: common ids found (oriented counts)
 #define C_PROBED 15 // ids probed by the oriented bitmap kernel
-#define C_ITEMS2 16 // bitmap items, the oriented kernel's second launch
-#define C_NUM 17
+#define C_NUM 16
 
 #define MERGE_WARPS 8        // warps per merge/gallop CTA
 #define ITEM_TARGET_DEFAULT (1u << 20)  // probe elements per bitmap work item
@@ -638,20 +637,19 @@ int accx_prefix_lengths(accx_graph *g, cudaStream_t s) {
 static int g_block_warps = 32;
 static int g_dense_kb = 128;
 static int g_sparse_kb = 64;
-static int g_or_dense_kb = 56;     // with 512-thread blocks two CTAs share an SM
+// Oriented bitmap kind: 256-thread CTAs, four per SM, with a 24 KiB window (owners
+// with ids below 196,608 use the bitmap kind, the others gallop).  Small CTAs run
+// a round's scans and barriers with fewer idle threads (most owners' rows are far
+// shorter than a CTA), and the low-degree owners past the window are cheaper to
+// gallop than to stage.  Whole counts (ms) by (CTA threads, window KiB):
+//   R-MAT 22: 256/24 18.9, 512/56 24.1 (the earlier default), 256/16 18.4
+//   R-MAT 24: 256/24 96.7, 512/56 98.6, 256/16 110.9 (too many owners gallop)
+//   Chung-Lu 20M (exponent 2.1): 256/24 46.0, 512/56 ~49; Erdos-Renyi 20M: 32.1, ~33.3
+// and with 256 threads a 32 KiB window (three CTAs per SM) or 128-thread CTAs
+// were slower at R-MAT 24 (95.4 and 93.5-127.4 ms for the bitmap phase alone).
+static int g_or_dense_kb = 24;
 static int g_or_counter_kb = 8;
-static int g_or_block_warps = 16;
-// The first (small-CTA) launch of the oriented bitmap kind: its window (KiB) and
-// CTA size.  R-MAT 24 bitmap phase by (window, CTA size): 12-24 KiB at 256
-// threads 81.2-81.7 ms (four CTAs per SM), 32 KiB 95.4 ms (three per SM), 16 and
-// 24 KiB at 128 threads 93.5 and 127.4 ms; one 512-thread launch 82.9 ms.
-#ifndef OR_SMALL_KB
-#define OR_SMALL_KB 24u
-#endif
-#ifndef OR_SMALL_NT
-#define OR_SMALL_NT 256
-#endif
-#define OR_SMALL_W (OR_SMALL_KB * 8192u)
+static int g_or_block_warps = 8;
 
 
 static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s) {
@@ -753,33 +751,16 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s)
     k_gallop_or<GALLOP_OR_GROUP><<<sms * 8, MERGE_WARPS * 32, 0, s>>>(off, dst, g->d_pre, g->d_rev, g->d_edge_list, list_cap, ctr,
                                                      cnt);
     ACCX_MARK(3);
-    // With the default shape the bitmap kind runs as two launches over the owner
-    // range: owners below OR_SMALL_W (their prefixes fit a 24 KiB window) in
-    // 256-thread CTAs, four per SM, whose smaller rounds and item set-up hide their
-    // barriers better (R-MAT 24: 67.6 ms for the owners below 131K ids, against
-    // 82.9 ms for all owners in 512-thread CTAs, two per SM); then the other owners
-    // below W with the full window.  Counts do not depend on the split.
-    const bool split = !(o && (o->block_warps > 0 || o->bitmap_window_kb > 0)) && W > OR_SMALL_W;
-    const uint32_t W1 = split ? OR_SMALL_W : 0u;
-    if (split) {
-      const size_t smem1 = (size_t)W1 / 8u + 16u + (size_t)pcap * 4u + (size_t)W1 / 16u;
-      auto k1 = k_bitmap_or<OR_SMALL_NT>;
-      ACCX_CUDA_TRY(cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
-      int per_sm1 = 0;
-      ACCX_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm1, k1, OR_SMALL_NT, smem1));
-      if (per_sm1 < 1) return ACCX_ERR_INVALID_ARG;
-      k1<<<sms * per_sm1, OR_SMALL_NT, smem1, s>>>(off, dst, g->d_pre, n, g->d_or_items, items_cap, work_u, g->d_prefix,
-                                           g->d_or_sl, W1, pcap, target, 0u, W1, C_ITEMS, cnt, ctr);
-    }
-    // blocks of up to 512 threads use the half-size instance (two CTAs per SM when
-    // shared memory allows)
-    auto kb = warps <= 16 ? k_bitmap_or<512> : k_bitmap_or<1024>;
+    // the instance whose per-round arrays fit the block: 256 threads (four CTAs per
+    // SM with the default 24 KiB window), 512 (two per SM with windows up to ~60
+    // KiB) or 1024
+    auto kb = warps <= 8 ? k_bitmap_or<256> : warps <= 16 ? k_bitmap_or<512> : k_bitmap_or<1024>;
     ACCX_CUDA_TRY(cudaFuncSetAttribute(kb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     ACCX_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb, warps * 32, smem));
     if (per_sm < 1) return ACCX_ERR_INVALID_ARG;
     kb<<<sms * per_sm, warps * 32, smem, s>>>(off, dst, g->d_pre, n, g->d_or_items, items_cap, work_u, g->d_prefix,
-                                              g->d_or_sl, W, pcap, target, W1, n, C_ITEMS2, cnt, ctr);
+                                              g->d_or_sl, W, pcap, target, cnt, ctr);
     ACCX_MARK(4);
     k_combine_or<<<tiles, 256, 0, s>>>(m, g->d_rev, cnt);
   } else {

@@ -227,8 +227,7 @@ __device__ __forceinline__ uint32_t or_piece(const int32_t *__restrict__ dst, ui
 // NT = the block size the per-round arrays are sized for (blockDim.x <= NT); a
 // 512-thread instance needs half the static shared memory, so two CTAs fit an
 // SM when the window is small enough, and a 256-thread one with a small window
-// runs four per SM.  A launch takes the items of the owners in [olo, ohi) (items
-// are in owner order), fetched through device counter ctr[cidx].
+// runs four per SM.
 template <int NT>
 __global__ void __launch_bounds__(NT, 1024 / NT) k_bitmap_or(const uint32_t *__restrict__ off,
                                                        const int32_t *__restrict__ dst,
@@ -237,8 +236,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bitmap_or(const uint32_t *__r
                                                        const unsigned long long *__restrict__ work_u,
                                                        const unsigned long long *__restrict__ prefix,
                                                        const uint2 *__restrict__ sl, uint32_t W, uint32_t pcap,
-                                                       uint32_t target, uint32_t olo, uint32_t ohi, int cidx,
-                                                       int32_t *__restrict__ cnt,
+                                                       uint32_t target, int32_t *__restrict__ cnt,
                                                        unsigned long long *__restrict__ ctr) {
   extern __shared__ __align__(16) uint32_t smem[];
   const uint32_t nwords = W / 32;
@@ -253,11 +251,10 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bitmap_or(const uint32_t *__r
   const int tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
   for (uint32_t i = tid; i <= nwords; i += nt) words[i] = 0;
-  const unsigned long long first = prefix[olo < n ? olo : n];
-  unsigned long long total = prefix[ohi < n ? ohi : n];
+  unsigned long long total = prefix[n];
   if (total > items_cap) total = items_cap;
   unsigned long long found = 0, probed = 0;  // this thread's share, summed per warp at the end
-  if (tid == 0) s_it = first + atomicAdd(&ctr[cidx], 1ull);
+  if (tid == 0) s_it = atomicAdd(&ctr[C_ITEMS], 1ull);
   __syncthreads();
   for (;;) {
     const unsigned long long it = s_it;
@@ -279,7 +276,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bitmap_or(const uint32_t *__r
       ocnt[i] = 0;
     }
     __syncthreads();
-    if (tid == 0) s_it = first + atomicAdd(&ctr[cidx], 1ull);  // the next item, read after this one
+    if (tid == 0) s_it = atomicAdd(&ctr[C_ITEMS], 1ull);  // the next item, read after this one
     for (uint32_t r0 = pa; r0 < pb; r0 += (uint32_t)nt) {
       const uint32_t k = r0 + (uint32_t)tid;
       uint32_t sst = 0, len = 0;

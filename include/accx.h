@@ -395,9 +395,7 @@ int accx_batch_launch(accx_batch *b, void *stream);
  * dense-window KiB, sparse-table KiB) for a policy on this graph and returns the
  * fastest in *best (other fields copied from *base).  all_ms (optional, >= 8
  * floats) receives each candidate's time, -1 for shapes the device cannot run.
- * For oriented counts one candidate is the default shape (all three 0), under
- * which the bitmap kind runs as a small-CTA launch for the lowest owners and a
- * full-window launch for the rest. */
+ * For oriented counts one candidate is the default shape (all three 0). */
 int accx_autotune(accx_graph *g, const accx_count_opts *base, int reps, accx_count_opts *best, float *best_ms,
                   float *all_ms, int *ncand, void *stream);
 

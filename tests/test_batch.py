@@ -80,7 +80,7 @@ def test_oriented_capture_and_autotune_match_eager():
     want = U.count(policy="bitmap", bias=2)
     s = torch.cuda.Stream()
     kw, ms, allms = U.autotune(policy="bitmap", reps=1, stream=s.cuda_stream, orient=True)
-    assert ms > 0 and kw["window_kb"] in (0, 32, 40, 48, 56, 64, 80)  # 0: the default (split) shape
+    assert ms > 0 and kw["window_kb"] in (0, 32, 40, 48, 56, 64, 80)  # 0: the library's default shape
     B.capture(policy="bitmap", bias=2, stream=s.cuda_stream, orient=True, **kw)
     for _ in range(2):
         U.count(policy="merge", bias=7, out=None)

@@ -144,6 +144,25 @@ def test_skew_config_scaled_down_parity_with_oracle(kind, default_sched):
         assert np.diff(off.astype(np.int64)).max() > 20_000  # the heavy head is there
 
 
+@pytest.mark.parametrize("kind", ["chung_lu", "erdos_renyi"])
+def test_skew_config_full_size_parity_with_oracle(kind, default_sched):
+    """The learned-scheduler skew config at full size: Chung-Lu with 20M vertices,
+    exponent 2.1, mean degree 24, max expected degree 1M (444.9M entries), and
+    Erdos-Renyi with 20M vertices, mean degree 24 (480.0M entries).  The
+    scheduler's tuned plan (as the bench runs it) and the reference's ratio-50
+    rule equal the oracle's CheckCoreBitmap (all host threads) entry for entry."""
+    from acctricnt_gb300 import workloads
+    p = workloads.chung_lu_20m() if kind == "chung_lu" else workloads.er_20m()
+    G = accx.Graph.generate(p)
+    off, dst = G.download()
+    ref = oracle.cn_count(off, dst, nthreads=0)
+    assert np.array_equal(G.count(policy="heuristic", bias=2), ref)
+    G.relabel()
+    pl = default_sched.plan(G, tune=True)
+    assert np.array_equal(G.count(policy="model", orient=pl["orient"], bias=2), ref)
+    G.free()
+
+
 def test_large_rmat_policies_agree_and_are_symmetric():
     """Size-independent properties at R-MAT scale 20: all policies agree, the
     count array is symmetric (cnt[e] == cnt[reverse(e)]), and sampled entries

@@ -89,7 +89,7 @@ class ServerStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
-SCHED_NOFFSETS = 8
+SCHED_NOFFSETS = 10
 
 
 class SchedConfig(C.Structure):

@@ -15,7 +15,7 @@
 //     library's own FP16/FP32 training kernels on the rows of seven seeded
 //     graphs, then calibrated on whole counts: per-bucket timings taken alone
 //     overstate the bitmap kind (its owner staging serves all of an owner's
-//     buckets), so one log2 offset for that kind is chosen among eight
+//     buckets), so one log2 offset for that kind is chosen among ten
 //     candidates by the size-weighted count time on the calibration graphs;
 //   * a plan attaches both models to a graph, predicts each mode's time from
 //     its own table and picks the faster mode; optionally it refines the
@@ -35,7 +35,12 @@
 #define NB ACCX_NB
 #define NBK (ACCX_NB * ACCX_NB)
 
-static const float kOffsets[ACCX_SCHED_NOFFSETS] = {0.0f, -0.5f, -1.0f, -1.5f, -2.0f, -3.0f, -5.0f, -64.0f};
+// Bitmap-kind log2 offsets: negative ones favour the bitmap kind (-64: every
+// bucket), positive ones the merge and galloping kinds (64: no bucket; on the
+// Erdos-Renyi graph, where owners have short prefixes, galloping everywhere is the
+// fastest fixed policy).
+static const float kOffsets[ACCX_SCHED_NOFFSETS] = {0.0f, -0.5f, -1.0f, -1.5f, -2.0f,
+                                                    -3.0f, -5.0f, -64.0f, 1.0f, 64.0f};
 
 struct accx_sched {
   accx_model *model[2] = {nullptr, nullptr};

@@ -320,7 +320,8 @@ int accx_graph_set_model_oriented(accx_graph *g, accx_model *m);
 int accx_bucket_timings(accx_graph *g, int orient, int reps, uint64_t min_edges, uint64_t *edges, float *ms,
                         void *stream);
 
-#define ACCX_SCHED_NOFFSETS 8   /* bitmap-kind offsets tried: 0, -0.5, -1, -1.5, -2, -3, -5, -64 */
+#define ACCX_SCHED_NOFFSETS 10  /* bitmap-kind log2 offsets tried: 0, -0.5, -1, -1.5, -2, -3, -5, -64
+                                   (-64: the bitmap kind for every bucket), 1, 64 (never the bitmap kind) */
 typedef struct accx_sched accx_sched;
 typedef struct {
   uint64_t seed;  /* model initialisation (0 = 1) */

@@ -78,6 +78,7 @@ struct accx_graph {
   uint32_t *d_or_items = nullptr;          // n + m/32 + 1 oriented bitmap work items: owner of each
   uint32_t *d_rev = nullptr;               // m reverse entry of every entry of the counting CSR (oriented counts)
   uint32_t *d_rev_orig = nullptr;          // m reverse entries of the handle's own CSR, recorded by full validation
+  bool symmetric = false;                  // known symmetric: validated, generated or built from an edge list
   const uint32_t *rev_csr = nullptr;       // the offsets array d_rev was built for
   void *d_scan_tmp = nullptr;
   size_t scan_tmp_bytes = 0;
@@ -142,6 +143,10 @@ int accx_model_plan_ms(accx_model *m, accx_graph *g, int mode, cudaStream_t s, d
 // Exclusive/inclusive helpers implemented in gen.cu.
 // Row index of every 256-entry tile of a CSR (graph.cu), allocated on g's home stream.
 int accx_tilerow_build(accx_graph *g, const uint32_t *off, uint32_t **out, cudaStream_t s);
+// Reverse index of g's CSR (off, tilerow, dst) by a stable sort of the entries
+// by neighbour id; with d_status the symmetry it relies on is checked (graph.cu).
+int accx_rev_by_sort(accx_graph *g, const uint32_t *off, const uint32_t *tilerow, const int32_t *dst, int *d_status,
+                     cudaStream_t s, uint32_t **rev_out);
 
 // Relabeled counts -> the handle's entry order (relabel.cu).
 int accx_relabel_gather(accx_graph *g, cudaStream_t s);

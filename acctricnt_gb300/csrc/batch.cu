@@ -56,12 +56,14 @@ extern "C" int accx_batch_create(accx_graph *const *graphs, int k, void *stream,
   if (!b) return ACCX_ERR_OOM;
   b->k = k;
   uint64_t N = 0, M = 0;
+  bool sym = true;  // the union is symmetric when every member is
   std::vector<accx_batch_desc> ds(k);
   for (int i = 0; i < k; i++) {
     if (!graphs[i]) {
       delete b;
       return ACCX_ERR_INVALID_ARG;
     }
+    sym = sym && graphs[i]->symmetric;
     ds[i] = {graphs[i]->d_off, graphs[i]->d_dst, graphs[i]->n, (uint32_t)N, graphs[i]->m, M};
     b->vbase.push_back((uint32_t)N);
     b->n.push_back(graphs[i]->n);
@@ -82,6 +84,7 @@ extern "C" int accx_batch_create(accx_graph *const *graphs, int k, void *stream,
   cudaGetDevice(&u->device);
   u->n = (uint32_t)N;
   u->m = M;
+  u->symmetric = sym;
   b->u = u;
   accx_batch_desc *d_ds = nullptr;
   int rc = ACCX_OK;

@@ -715,26 +715,40 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s)
     // per-entry bitmap work and the item array (n + m/32 + 1 bounds the items:
     // an owner is cut into at most max(1, degree/32) slices)
     const uint32_t items_cap = n + m / 32u + 1u;
-    if (!g->d_or_sl || !g->d_or_items || !g->d_rev) {
+    if (!g->d_or_sl || !g->d_or_items) {
       if (!g->d_or_sl) ACCX_CUDA_TRY(accx_dev_alloc((void **)&g->d_or_sl, sizeof(uint2) * (size_t)m, g->home));
       if (!g->d_or_items)
         ACCX_CUDA_TRY(accx_dev_alloc((void **)&g->d_or_items, sizeof(uint32_t) * (size_t)items_cap, g->home));
-      if (!g->d_rev) ACCX_CUDA_TRY(accx_dev_alloc((void **)&g->d_rev, sizeof(uint32_t) * (size_t)m, g->home));
-      g->rev_csr = nullptr;
       if (g->home) ACCX_CUDA_TRY(cudaStreamSynchronize(g->home));
     }
     k_fill<<<sms * 8, 256, 0, s>>>(cnt, m, bias);
     k_pre<<<sms * 8, 256, 0, s>>>(off, dst, n, g->d_pre);
     // reverse entries: built on the first oriented count of this CSR and kept
-    // (an index of the graph, like the tile rows)
+    // (an index of the graph, like the tile rows).  The original CSR's comes
+    // from validation; a known-symmetric CSR's from the sort (accx_rev_by_sort);
+    // otherwise, or when the sort's scratch does not fit, a search per entry
+    // pair, which leaves 0xffffffff where an asymmetric CSR has no reverse.
     if (g->rev_csr != off) {
+      uint32_t *sorted = nullptr;
       if (g->d_rev_orig && !rel) {  // recorded by validation for this very CSR
-        ACCX_CUDA_TRY(cudaMemcpyAsync(g->d_rev, g->d_rev_orig, sizeof(uint32_t) * (size_t)m, cudaMemcpyDeviceToDevice, s));
-      } else if (g->d_rev_orig) {
-        k_rev_compose<<<sms * 8, 256, 0, s>>>(g->d_rmap, g->d_rev_orig, m, g->d_rev);
+        std::swap(g->d_rev, g->d_rev_orig);
+        accx_dev_free(g->d_rev_orig, g->home);
+        g->d_rev_orig = nullptr;
       } else {
-        ACCX_CUDA_TRY(cudaMemsetAsync(g->d_rev, 0xff, sizeof(uint32_t) * (size_t)m, s));
-        k_rev_build<256><<<tiles, 256, 0, s>>>(off, tilerow, dst, g->d_pre, n, m, g->d_rev);
+        rc = g->symmetric ? accx_rev_by_sort(g, off, tilerow, dst, nullptr, s, &sorted) : ACCX_ERR_OOM;
+        if (rc == ACCX_OK) {
+          accx_dev_free(g->d_rev, g->home);
+          g->d_rev = sorted;
+        } else if (rc == ACCX_ERR_OOM) {
+          if (!g->d_rev) {
+            ACCX_CUDA_TRY(accx_dev_alloc((void **)&g->d_rev, sizeof(uint32_t) * (size_t)m, g->home));
+            if (g->home) ACCX_CUDA_TRY(cudaStreamSynchronize(g->home));
+          }
+          ACCX_CUDA_TRY(cudaMemsetAsync(g->d_rev, 0xff, sizeof(uint32_t) * (size_t)m, s));
+          k_rev_build<256><<<tiles, 256, 0, s>>>(off, tilerow, dst, g->d_pre, n, m, g->d_rev);
+        } else {
+          return rc;
+        }
       }
       g->rev_csr = off;
     }

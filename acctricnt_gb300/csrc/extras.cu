@@ -39,6 +39,7 @@ extern "C" int accx_graph_from_edges(const uint32_t *src, const uint32_t *dst, u
   accx_graph *g = new (std::nothrow) accx_graph();
   if (!g) return ACCX_ERR_OOM;
   cudaGetDevice(&g->device);
+  g->symmetric = true;  // both directions of every edge are kept
   unsigned long long *keys = nullptr;
   uint32_t *ds = nullptr, *dd = nullptr;
   int *bad = nullptr, hbad = 0;

@@ -109,6 +109,7 @@ extern "C" int accx_graph_generate(const accx_gen_params *p, void *stream, accx_
   if (!g) return ACCX_ERR_OOM;
   cudaGetDevice(&g->device);
   g->home = s;
+  g->symmetric = true;  // the edge stream is symmetrised
   unsigned long long *d_keys = nullptr;
   uint64_t *d_cdf = nullptr;
   do {

@@ -9,6 +9,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <cub/cub.cuh>
+
 #include <mutex>
 #include <string>
 #include <vector>
@@ -194,13 +196,16 @@ int accx_grid_for(int device, int block, int per_sm) {
 #define V_UNSORTED 4
 #define V_ASYM 8
 // Range checks always run (every kernel indexes off[] with neighbour ids); the
-// order, self-loop and symmetry checks run when `full` is set.  Symmetry: of the
+// order and self-loop checks run when `full` is set.  Symmetry is checked after
+// this pass by sorting the entries by neighbour id (k_rev_check).  SEARCH: the
+// fallback when the sort's buffers do not fit, a search per entry pair -- of the
 // two entries of a pair only the one whose target has the smaller degree (ties:
 // the larger target id) searches its reverse, in that shorter list, and the
 // searching entries are counted.  If every searching entry finds its reverse (a
 // non-searching entry; distinct entries have distinct reverses in sorted lists
 // without repeats) and they are exactly half of all entries, the reverse map is a
 // bijection onto the other half: the graph is symmetric.
+template <bool SEARCH>
 __global__ void k_validate(const uint32_t *__restrict__ off, const uint32_t *__restrict__ tilerow, const int32_t *__restrict__ dst, uint32_t n,
                            uint32_t m, int full, int *__restrict__ status, unsigned long long *__restrict__ searched,
                            uint32_t *__restrict__ rev) {
@@ -219,7 +224,7 @@ __global__ void k_validate(const uint32_t *__restrict__ off, const uint32_t *__r
         flag = V_SELF;
       } else if (e > off[u] && dst[e - 1] >= v) {
         flag = V_UNSORTED;
-      } else {
+      } else if (SEARCH) {
         const uint32_t du = off[u + 1] - off[u], b = off[v], t = off[v + 1], dv = t - b;
         chk = dv < du || (dv == du && (uint32_t)v > u);
         if (chk) {
@@ -235,10 +240,101 @@ __global__ void k_validate(const uint32_t *__restrict__ off, const uint32_t *__r
     }
   }
   if (flag) atomicOr(status, flag);
-  if (full) {  // uniform over the block
+  if (SEARCH && full) {  // uniform over the block
     const int c = __syncthreads_count(chk);
     if (threadIdx.x == 0 && c) atomicAdd(searched, (unsigned long long)c);
   }
+}
+
+__global__ void k_iota(uint32_t *__restrict__ v, uint32_t m) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) v[i] = i;
+}
+
+// The reverse index by a stable radix sort of (neighbour id, entry index) pairs
+// over the id bits.  The sort keeps the row order (w ascending) of the entries
+// (w, v) of one neighbour v, so on a symmetric CSR with sorted rows the run of v
+// is row v's place and the entry sorted to place i is the reverse of entry i:
+// the sorted indices ARE the reverse index (an involution, so it is its own
+// inverse).  k_rev_check verifies that premise at every place i instead of
+// assuming it:
+//   key[i] == row(i)                    every vertex is the neighbour in as many
+//                                       entries as its own row is long;
+//   off[dst[i]] <= rev[i] < off[dst[i]+1]  the entry e = rev[i] = (w, v) sorted
+//                                       to place i lies in the row of place i's
+//                                       neighbour: w = dst[i].
+// Together entry i = (v, w) is the reverse of e, and since rev is a permutation
+// of [0, m) every entry has its reverse: the graph is symmetric.  The second
+// test reads off[] at neighbour ids, an array of 4(n+1) bytes that the L2 holds
+// for graphs of up to ~30M vertices, where a test through rev itself would be a
+// random read of the 4m-byte index.
+__global__ void __launch_bounds__(256) k_rev_check(const uint32_t *__restrict__ off, const uint32_t *__restrict__ tilerow,
+                                                   const int32_t *__restrict__ dst, uint32_t n, uint32_t m,
+                                                   const uint32_t *__restrict__ key, const uint32_t *__restrict__ rev,
+                                                   int *__restrict__ status) {
+  __shared__ accx_tile_rows<256> sh;
+  const uint32_t base = blockIdx.x * 256u;
+  const uint32_t i = base + threadIdx.x;
+  const uint32_t u = accx_tile_row<256>(off, tilerow, n, m, base, i, &sh);
+  if (i < m) {
+    const uint32_t v = (uint32_t)dst[i], r = rev[i];  // v < n: the range check ran first
+    if (key[i] != u || r < __ldg(off + v) || r >= __ldg(off + v + 1)) atomicOr(status, V_ASYM);
+  }
+}
+
+// The sort behind k_rev_check, for the CSR (off, tilerow, dst) of g with g->m
+// entries, all ids already range-checked.  About 16 bytes per entry of scratch.
+// With d_status the premise is checked (defects OR-ed into *d_status, the caller
+// reads it); without it the CSR must be known symmetric.  On success *rev_out is
+// a new device array (the caller owns it) -- valid as a reverse index only if
+// the check passed or the CSR is symmetric.  Returns ACCX_ERR_OOM, before any
+// work, when the scratch does not fit.
+int accx_rev_by_sort(accx_graph *g, const uint32_t *off, const uint32_t *tilerow, const int32_t *dst, int *d_status,
+                     cudaStream_t s, uint32_t **rev_out) {
+  const uint32_t m = (uint32_t)g->m;
+  *rev_out = nullptr;
+  if (!m) return ACCX_OK;
+  int bits = 1;
+  while (bits < 32 && (1ull << bits) < (unsigned long long)g->n) bits++;
+  uint32_t *buf[4] = {nullptr, nullptr, nullptr, nullptr};
+  void *tmp = nullptr;
+  size_t tb = 0;
+  cub::DoubleBuffer<uint32_t> dk(nullptr, nullptr), dv(nullptr, nullptr);
+  if (cub::DeviceRadixSort::SortPairs(nullptr, tb, dk, dv, (int64_t)m, 0, bits, s) != cudaSuccess) {
+    accx_set_cuda_error(cudaGetLastError(), "rev sort", __FILE__, __LINE__);
+    return ACCX_ERR_CUDA;
+  }
+  bool room = true;
+  for (int i = 0; i < 4 && room; i++)
+    room = accx_dev_alloc((void **)&buf[i], sizeof(uint32_t) * (size_t)m, nullptr) == cudaSuccess;
+  if (room) room = accx_dev_alloc(&tmp, tb + 16, nullptr) == cudaSuccess;
+  if (!room) {
+    cudaGetLastError();
+    for (uint32_t *p : buf) accx_dev_free(p, nullptr);
+    accx_dev_free(tmp, nullptr);
+    return ACCX_ERR_OOM;
+  }
+  int rc = ACCX_OK;
+  dk = cub::DoubleBuffer<uint32_t>(buf[0], buf[1]);
+  dv = cub::DoubleBuffer<uint32_t>(buf[2], buf[3]);
+  if (cudaMemcpyAsync(buf[0], dst, sizeof(uint32_t) * (size_t)m, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+    rc = ACCX_ERR_CUDA;
+  if (!rc) {
+    k_iota<<<accx_sm_count(g->device) * 8, 256, 0, s>>>(buf[2], m);
+    if (cub::DeviceRadixSort::SortPairs(tmp, tb, dk, dv, (int64_t)m, 0, bits, s) != cudaSuccess) rc = ACCX_ERR_CUDA;
+  }
+  if (!rc && d_status)
+    k_rev_check<<<(m + 255) / 256, 256, 0, s>>>(off, tilerow, dst, g->n, m, dk.Current(), dv.Current(), d_status);
+  if (!rc && (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess)) rc = ACCX_ERR_CUDA;
+  if (rc) {
+    accx_set_cuda_error(cudaGetLastError(), "rev sort", __FILE__, __LINE__);
+    cudaStreamSynchronize(s);  // nothing may still read the buffers
+  }
+  uint32_t *keep = rc ? nullptr : dv.Current();
+  for (uint32_t *p : buf)
+    if (p != keep) accx_dev_free(p, nullptr);
+  accx_dev_free(tmp, nullptr);
+  *rev_out = keep;
+  return rc;
 }
 
 __global__ void k_tilerow(const uint32_t *__restrict__ off, uint32_t n, uint32_t m, uint32_t ntiles,
@@ -263,13 +359,6 @@ int accx_tilerow_build(accx_graph *g, const uint32_t *off, uint32_t **out, cudaS
   return ACCX_OK;
 }
 
-static int check_offsets_host(const uint32_t *off, uint32_t n, uint64_t m) {
-  if (off[0] != 0 || off[n] != m) return ACCX_ERR_RANGE;
-  for (uint32_t i = 0; i < n; i++)
-    if (off[i + 1] < off[i]) return ACCX_ERR_RANGE;
-  return ACCX_OK;
-}
-
 __global__ void k_check_offsets(const uint32_t *__restrict__ off, uint32_t n, uint32_t m, int *status) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     if (off[i + 1] < off[i]) atomicOr(status, V_RANGE);
@@ -290,27 +379,52 @@ int accx_graph_validate_device(accx_graph *g, int full, cudaStream_t s) {
         cudaStreamSynchronize(s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
     if (st) { rc = ACCX_ERR_RANGE; break; }
     if ((rc = accx_tilerow_build(g, g->d_off, &g->d_tilerow, s)) != ACCX_OK) break;
-    if (g->m) {
-      uint32_t blocks = (uint32_t)((g->m + 255) / 256);
+    if (!g->m) break;
+    const uint32_t blocks = (uint32_t)((g->m + 255) / 256);
+    k_validate<false><<<blocks, 256, 0, s>>>(g->d_off, g->d_tilerow, g->d_dst, g->n, (uint32_t)g->m, full, d_status,
+                                             nullptr, nullptr);
+    if (cudaMemcpyAsync(&st, d_status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
+    if (full && !st) {
+      // symmetry, and with it the reverse index, by the sort; by a search per
+      // entry pair when its scratch does not fit
       uint32_t *rev = nullptr;
-      if (full && !g->d_rev_orig && accx_dev_alloc((void **)&rev, sizeof(uint32_t) * (size_t)g->m, nullptr) != cudaSuccess) {
-        cudaGetLastError();
-        rev = nullptr;  // no room: counts build the index themselves
+      rc = g->d_rev_orig ? ACCX_ERR_OOM : accx_rev_by_sort(g, g->d_off, g->d_tilerow, g->d_dst, d_status, s, &rev);
+      if (rc == ACCX_ERR_OOM) {
+        rc = ACCX_OK;
+        if (!g->d_rev_orig && accx_dev_alloc((void **)&rev, sizeof(uint32_t) * (size_t)g->m, nullptr) != cudaSuccess) {
+          cudaGetLastError();
+          rev = nullptr;  // no room: counts build the index themselves
+        }
+        k_validate<true><<<blocks, 256, 0, s>>>(g->d_off, g->d_tilerow, g->d_dst, g->n, (uint32_t)g->m, full, d_status,
+                                                d_searched, rev);
+        unsigned long long searched = 0;
+        if (cudaMemcpyAsync(&st, d_status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaMemcpyAsync(&searched, d_searched, sizeof(searched), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess) {
+          accx_dev_free(rev, nullptr);
+          rc = ACCX_ERR_CUDA;
+          break;
+        }
+        if (!st && 2 * searched != g->m) st = V_ASYM;
+      } else if (rc == ACCX_OK) {
+        if (cudaMemcpyAsync(&st, d_status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess) {
+          accx_dev_free(rev, nullptr);
+          rc = ACCX_ERR_CUDA;
+          break;
+        }
+      } else {
+        break;
       }
-      k_validate<<<blocks, 256, 0, s>>>(g->d_off, g->d_tilerow, g->d_dst, g->n, (uint32_t)g->m, full, d_status,
-                                        d_searched, rev);
-      unsigned long long searched = 0;
-      if (cudaMemcpyAsync(&st, d_status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-          cudaMemcpyAsync(&searched, d_searched, sizeof(searched), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-          cudaStreamSynchronize(s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
-      if (full && !st && 2 * searched != g->m) st = V_ASYM;
-      rc = (st & V_RANGE) ? ACCX_ERR_RANGE : (st & V_SELF) ? ACCX_ERR_SELF_LOOP
-         : (st & V_UNSORTED) ? ACCX_ERR_UNSORTED : (st & V_ASYM) ? ACCX_ERR_ASYMMETRIC : ACCX_OK;
       if (rev) {
-        if (rc == ACCX_OK) g->d_rev_orig = rev;  // complete only for a graph that passed
+        if (!st) g->d_rev_orig = rev;  // complete only for a graph that passed
         else accx_dev_free(rev, nullptr);
       }
+      if (!st) g->symmetric = true;
     }
+    rc = (st & V_RANGE) ? ACCX_ERR_RANGE : (st & V_SELF) ? ACCX_ERR_SELF_LOOP
+       : (st & V_UNSORTED) ? ACCX_ERR_UNSORTED : (st & V_ASYM) ? ACCX_ERR_ASYMMETRIC : ACCX_OK;
   } while (0);
   cudaFree(d_status);
   if (rc == ACCX_ERR_CUDA) accx_set_cuda_error(cudaGetLastError(), "validate", __FILE__, __LINE__);
@@ -351,11 +465,8 @@ extern "C" int accx_graph_create(const uint32_t *off, const int32_t *dst, uint32
   if (!off || (!dst && m) || !out) return ACCX_ERR_INVALID_ARG;
   *out = nullptr;
   cudaStream_t s = (cudaStream_t)stream;
-  bool off_dev = accx_is_device_ptr(off);
-  if (!off_dev) {
-    int rc = check_offsets_host(off, n, m);
-    if (rc) return rc;
-  }
+  // the offsets are checked on the device (k_check_offsets) before any kernel
+  // indexes with them
   accx_graph *g = nullptr;
   int rc = alloc_graph(n, m, &g);
   if (rc) return rc;

@@ -18,6 +18,7 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "accx_internal.h"
@@ -201,55 +202,126 @@ __global__ void __launch_bounds__(256) k_model_infer(const __half *__restrict__ 
 }
 
 // ---------------------------------------------------------------------------
-// Bucket statistics over owned edges: per block shared histograms, then global.
+// Bucket statistics over owned edges, both modes in one pass over the CSR counts
+// run on: [0] direct (owners and buckets by degree), [1] oriented (by prefix
+// length pre[], edges whose smaller prefix is empty left out -- the edges and
+// sizes oriented counting works on).  Direct statistics do not depend on the
+// vertex numbering: the owner is the endpoint of larger degree, and on a tie the
+// bucket and both sizes are the same whichever endpoint owns, so the relabeled
+// CSR gives the original CSR's figures.
 #define NBB (ACCX_NB * ACCX_NB)
-// ORIENT: owners and buckets by prefix length (pre), edges whose smaller prefix is
-// empty left out -- the edges and sizes oriented counting works on.
-template <int TILE, bool ORIENT>
-__global__ void __launch_bounds__(TILE) k_bucket_stats(const uint32_t *__restrict__ off, const uint32_t *__restrict__ tilerow, const int32_t *__restrict__ dst,
-                                                       uint32_t n, uint32_t m, unsigned long long *__restrict__ st,
-                                                       const uint32_t *__restrict__ pre) {
-  __shared__ accx_tile_rows<TILE> sh;
-  __shared__ unsigned long long hs[3 * NBB];
-  for (int i = threadIdx.x; i < 3 * NBB; i += TILE) hs[i] = 0;
-  // many tiles per CTA: the shared histograms reach the device counters once per CTA
-  const uint32_t ntiles = (m + TILE - 1) / TILE;
-  for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-  __syncthreads();
-  uint32_t base = tile * (uint32_t)TILE;
-  uint32_t e = base + threadIdx.x;
-  uint32_t u = accx_tile_row_at<TILE>(off, tilerow, n, m, tile, base, e, &sh);  // contains __syncthreads
+#define BS_EPT 8  // consecutive entries per thread
+
+// A thread's current run of one bucket, added to the CTA's histograms (count,
+// owner sizes, other sizes) when the bucket changes.  Runs are long: within a
+// row the partners come in id order, which after the relabel is degree order.
+struct bs_run {
   int b = -1;
-  uint32_t du = 0, dv = 0;
-  if (e < m) {
-    uint32_t v = (uint32_t)dst[e];
-    if (ORIENT) {
-      du = pre[u];
-      dv = pre[v];
-    } else {
-      du = off[u + 1] - off[u];
-      dv = off[v + 1] - off[v];
+  uint32_t c = 0;
+  unsigned long long so = 0, sp = 0;
+  __device__ __forceinline__ void flush(unsigned long long *h) {
+    if (c) {
+      atomicAdd(&h[b], (unsigned long long)c);
+      atomicAdd(&h[NBB + b], so);
+      atomicAdd(&h[2 * NBB + b], sp);
     }
-    if ((!ORIENT || dv > 0) && accx_owns(u, du, v, dv)) b = accx_bucket(du) * ACCX_NB + accx_bucket(dv);
+    c = 0;
+    so = sp = 0;
   }
-  // lanes of one bucket add up first (most of a warp lands in a few buckets);
-  // sizes are summed as 16-bit halves, so 32 lanes cannot overflow 32 bits
-  const unsigned peers = __match_any_sync(ACCX_FULL_MASK, b);
-  if (b >= 0) {
-    const unsigned long long su = ((unsigned long long)__reduce_add_sync(peers, du >> 16) << 16) +
-                                  __reduce_add_sync(peers, du & 0xffffu);
-    const unsigned long long sv = ((unsigned long long)__reduce_add_sync(peers, dv >> 16) << 16) +
-                                  __reduce_add_sync(peers, dv & 0xffffu);
-    if ((threadIdx.x & 31) == __ffs(peers) - 1) {
-      atomicAdd(&hs[b], (unsigned long long)__popc(peers));
-      atomicAdd(&hs[NBB + b], su);
-      atomicAdd(&hs[2 * NBB + b], sv);
+  // The chunk's last run: lanes holding the same bucket add up first (a warp's
+  // lanes mostly end in a few buckets, and same-address shared atomics from one
+  // warp serialise).  Sizes are summed as 16-bit halves, so 32 lanes of at most
+  // BS_EPT sizes each cannot overflow 32 bits.
+  __device__ __forceinline__ void flush_warp(unsigned long long *h) {
+    const unsigned act = __activemask();
+    const int key = c ? b : -1;
+    const unsigned peers = __match_any_sync(act, key);
+    if (key >= 0) {
+      const unsigned long long n = __reduce_add_sync(peers, c);
+      const unsigned long long o = ((unsigned long long)__reduce_add_sync(peers, (unsigned)(so >> 16)) << 16) +
+                                   __reduce_add_sync(peers, (unsigned)(so & 0xffffu));
+      const unsigned long long q = ((unsigned long long)__reduce_add_sync(peers, (unsigned)(sp >> 16)) << 16) +
+                                   __reduce_add_sync(peers, (unsigned)(sp & 0xffffu));
+      if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) {
+        atomicAdd(&h[b], n);
+        atomicAdd(&h[NBB + b], o);
+        atomicAdd(&h[2 * NBB + b], q);
+      }
     }
+    c = 0;
+    so = sp = 0;
   }
+  __device__ __forceinline__ void add(unsigned long long *h, int nb, uint32_t o, uint32_t p) {
+    if (nb != b) {
+      flush(h);
+      b = nb;
+    }
+    c++;
+    so += o;
+    sp += p;
+  }
+};
+
+// CTAs loop over tiles of NT*BS_EPT entries and reach the device counters once.
+template <int NT>
+__global__ void __launch_bounds__(NT) k_bucket_stats(const uint32_t *__restrict__ off, const uint32_t *__restrict__ tilerow,
+                                                     const int32_t *__restrict__ dst, uint32_t n, uint32_t m,
+                                                     const uint32_t *__restrict__ pre,
+                                                     unsigned long long *__restrict__ st_direct,
+                                                     unsigned long long *__restrict__ st_orient) {
+  static_assert((NT * BS_EPT) % 256 == 0, "tiles of whole tile-row tiles");
+  __shared__ unsigned long long hs[2][3 * NBB];
+  __shared__ uint32_t s_lo, s_hi;
+  for (int i = threadIdx.x; i < 6 * NBB; i += NT) (&hs[0][0])[i] = 0;
+  const uint32_t span = NT * BS_EPT;
+  const uint32_t ntiles = (uint32_t)(((unsigned long long)m + span - 1) / span);
+  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const uint32_t base = t * span;
+    __syncthreads();  // the histograms' clearing, and the last tile's row range read
+    if (threadIdx.x == 0) {
+      // tilerow[k] = the row of entry 256k, its last element the row of entry m-1
+      const uint32_t last = (base + span < m ? base + span : m) - 1;
+      s_lo = __ldg(tilerow + base / 256u);
+      s_hi = __ldg(tilerow + last / 256u + 1u);
+    }
+    __syncthreads();
+    const uint32_t e0 = base + threadIdx.x * BS_EPT;
+    if (e0 >= m) continue;
+    const uint32_t e1 = e0 + BS_EPT < m ? e0 + BS_EPT : m;
+    // the partners' sizes first (independent loads in flight), then the rows
+    uint32_t vv[BS_EPT], dd[BS_EPT], pp[BS_EPT];
+#pragma unroll
+    for (int j = 0; j < BS_EPT; j++) vv[j] = e0 + j < e1 ? (uint32_t)__ldg(dst + e0 + j) : 0u;
+#pragma unroll
+    for (int j = 0; j < BS_EPT; j++) {
+      dd[j] = __ldg(off + vv[j] + 1) - __ldg(off + vv[j]);
+      pp[j] = __ldg(pre + vv[j]);
+    }
+    uint32_t u = accx_row_of(off, s_lo, s_hi + 1, e0);
+    uint32_t rb = __ldg(off + u), re = __ldg(off + u + 1), pu = __ldg(pre + u);
+    bs_run rd, ro;
+#pragma unroll
+    for (int j = 0; j < BS_EPT; j++) {
+      const uint32_t e = e0 + j;
+      if (e >= e1) break;
+      while (re <= e) {  // the next non-empty row
+        u++;
+        rb = re;
+        re = __ldg(off + u + 1);
+        pu = __ldg(pre + u);
+      }
+      const uint32_t v = vv[j], du = re - rb, dv = dd[j], pv = pp[j];
+      if (accx_owns(u, du, v, dv)) rd.add(hs[0], accx_bucket(du) * ACCX_NB + accx_bucket(dv), du, dv);
+      if (pv > 0 && accx_owns(u, pu, v, pv)) ro.add(hs[1], accx_bucket(pu) * ACCX_NB + accx_bucket(pv), pu, pv);
+    }
+    rd.flush_warp(hs[0]);
+    ro.flush_warp(hs[1]);
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < 3 * NBB; i += TILE)
-    if (hs[i]) atomicAdd(&st[i], hs[i]);
+  for (int i = threadIdx.x; i < 3 * NBB; i += NT) {
+    if (hs[0][i]) atomicAdd(&st_direct[i], hs[0][i]);
+    if (hs[1][i]) atomicAdd(&st_orient[i], hs[1][i]);
+  }
 }
 
 __device__ __forceinline__ void accx_feature_row(const unsigned long long *st, int b, uint32_t n, uint64_t m,
@@ -308,30 +380,40 @@ void accx_model_release(accx_graph *g) {
   g->model = nullptr;
 }
 
+// Both modes' statistics and features at once, on the CSR counts run on (the
+// relabeled one when the handle has it); recomputed when that changes.
 static int ensure_features(accx_graph *g, cudaStream_t s, int mode) {
   accx_graph_model_state *st = state_of(g);
   if (!st) return ACCX_ERR_OOM;
-  const bool rel = mode == 1 && g->d_roff != nullptr;
+  const bool rel = g->d_roff != nullptr;
   const uint32_t *off = rel ? g->d_roff : g->d_off;
   if (st->ready[mode] && st->csr[mode] == off) return ACCX_OK;
-  if (!st->d_stats[mode]) ACCX_CUDA_TRY(cudaMalloc(&st->d_stats[mode], sizeof(unsigned long long) * 3 * NBB));
-  if (!st->d_feat[mode]) ACCX_CUDA_TRY(cudaMalloc(&st->d_feat[mode], sizeof(float) * NBB * IN));
-  ACCX_CUDA_TRY(cudaMemsetAsync(st->d_stats[mode], 0, sizeof(unsigned long long) * 3 * NBB, s));
+  for (int k = 0; k < 2; k++) {
+    if (!st->d_stats[k]) ACCX_CUDA_TRY(cudaMalloc(&st->d_stats[k], sizeof(unsigned long long) * 3 * NBB));
+    if (!st->d_feat[k]) ACCX_CUDA_TRY(cudaMalloc(&st->d_feat[k], sizeof(float) * NBB * IN));
+    ACCX_CUDA_TRY(cudaMemsetAsync(st->d_stats[k], 0, sizeof(unsigned long long) * 3 * NBB, s));
+  }
   const uint32_t m = (uint32_t)g->m;
-  if (mode == 0) {
-    if (m) k_bucket_stats<256, false><<<min((m + 255) / 256, (uint32_t)accx_sm_count(g->device) * 8), 256, 0, s>>>(g->d_off, g->d_tilerow, g->d_dst, g->n, m,
-                                                                    st->d_stats[0], nullptr);
-  } else if (m) {
+  if (m) {
     int rc = accx_prefix_lengths(g, s);
     if (rc) return rc;
-    k_bucket_stats<256, true><<<min((m + 255) / 256, (uint32_t)accx_sm_count(g->device) * 8), 256, 0, s>>>(off, rel ? g->d_rtilerow : g->d_tilerow,
-                                                             rel ? g->d_rdst : g->d_dst, g->n, m, st->d_stats[1],
-                                                             g->d_pre);
+    const uint32_t *tilerow = rel ? g->d_rtilerow : g->d_tilerow;
+    if (!tilerow) {
+      rc = accx_tilerow_build(g, off, rel ? &g->d_rtilerow : &g->d_tilerow, s);
+      if (rc) return rc;
+      tilerow = rel ? g->d_rtilerow : g->d_tilerow;
+    }
+    const uint32_t tiles = (uint32_t)(((unsigned long long)m + 256 * BS_EPT - 1) / (256 * BS_EPT));
+    const uint32_t grid = std::min(tiles, (uint32_t)accx_sm_count(g->device) * 4);
+    k_bucket_stats<256><<<grid, 256, 0, s>>>(off, tilerow, rel ? g->d_rdst : g->d_dst, g->n, m, g->d_pre,
+                                             st->d_stats[0], st->d_stats[1]);
   }
-  k_features<<<(NBB + 127) / 128, 128, 0, s>>>(st->d_stats[mode], g->n, g->m, st->d_feat[mode]);
+  for (int k = 0; k < 2; k++) {
+    k_features<<<(NBB + 127) / 128, 128, 0, s>>>(st->d_stats[k], g->n, g->m, st->d_feat[k]);
+    st->ready[k] = true;
+    st->csr[k] = off;
+  }
   ACCX_CUDA_TRY(cudaGetLastError());
-  st->ready[mode] = true;
-  st->csr[mode] = off;
   return ACCX_OK;
 }
 

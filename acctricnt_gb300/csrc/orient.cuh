@@ -57,14 +57,6 @@ __global__ void __launch_bounds__(TILE) k_rev_build(const uint32_t *__restrict__
   }
 }
 
-// Reverse entries of the relabeled CSR from those of the original one:
-// rev_rel[map[e]] = map[rev[e]].
-__global__ void k_rev_compose(const uint32_t *__restrict__ map, const uint32_t *__restrict__ rev, uint32_t m,
-                              uint32_t *__restrict__ rev_rel) {
-  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < m; e += gridDim.x * blockDim.x)
-    rev_rel[__ldg(map + e)] = __ldg(map + __ldg(rev + e));
-}
-
 // The two prefix ranges of an owned edge (x owner, y = dst[e]), each cut at
 // min(x, y): ids from there up cannot be common to both prefixes.  The cut of
 // P(x) at y < x is the entry e itself; the cut of P(y) at x < y is x's position

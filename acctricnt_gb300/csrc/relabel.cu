@@ -276,6 +276,10 @@ extern "C" int accx_graph_relabel(accx_graph *g, void *stream) {
   for (void *p : {(void *)vkeys, (void *)vkeys2, (void *)key, (void *)val, (void *)key2, (void *)val2, (void *)rdeg,
                   (void *)bounds, tmp})
     accx_dev_free(p, g->home);
+  if (!rc && g->d_rev_orig) {  // counts run on the relabeled CSR from now on
+    accx_dev_free(g->d_rev_orig, g->home);
+    g->d_rev_orig = nullptr;
+  }
   if (rc) {
     for (void **p : {(void **)&g->d_roff, (void **)&g->d_rdst, (void **)&g->d_rmap, (void **)&g->d_rcnt,
                      (void **)&g->d_oldid, (void **)&g->d_newid, (void **)&g->d_rtilerow}) {

@@ -275,6 +275,34 @@ def test_invalid_graphs_rejected(bad):
     assert ei.value.status == code
 
 
+@pytest.mark.parametrize("case", ["directed_cycle", "swapped_targets"])
+def test_asymmetric_graphs_with_balanced_degrees_rejected(case):
+    """Every vertex is a neighbour as often as its own list is long, yet the
+    graph is not symmetric: the row-of-neighbour test of the sorted check (not
+    the degree test) has to catch these."""
+    if case == "directed_cycle":
+        off, dst = np.array([0, 1, 2, 3], np.uint32), np.array([1, 2, 0], np.int32)
+    else:  # the edges 0-1 and 2-3 with one target of each pair swapped
+        off, dst = np.array([0, 1, 2, 3, 4], np.uint32), np.array([3, 0, 1, 2], np.int32)
+    with pytest.raises(accx.AccxError) as ei:
+        accx.Graph.from_csr(off, dst)
+    assert ei.value.status == accx.ERR_ASYMMETRIC
+
+
+@pytest.mark.parametrize("validate", [True, False])
+def test_reverse_index_sources_give_the_same_counts(validate):
+    """The oriented count's reverse index comes from validation (validated
+    handle, original CSR), from the sort (relabeled CSR of a known-symmetric
+    handle) or from the search (an unvalidated handle): the same counts."""
+    off, dst = accx.generate_host(accx.rmat_params(14, 16, seed=8))
+    ref = oracle.cn_count(off, dst, 2)
+    G = accx.Graph.from_csr(off, dst, validate=validate)
+    assert np.array_equal(G.count(policy="bitmap", bias=2, orient=True), ref)
+    G.relabel()
+    assert np.array_equal(G.count(policy="bitmap", bias=2, orient=True), ref)
+    G.free()
+
+
 def test_query_before_count_is_not_ready():
     off, dst = accx.generate_host(accx.rmat_params(8, 8))
     G = accx.Graph.from_csr(off, dst)

@@ -110,6 +110,36 @@ def test_oriented_bucket_stats_match_numpy():
     assert np.array_equal(so, rso) and np.array_equal(sp, rsp)
 
 
+def _np_direct_stats(off, dst):
+    """Direct bucket statistics restated in numpy: owner = larger degree (ties:
+    smaller id)."""
+    n = len(off) - 1
+    deg = np.diff(off).astype(np.int64)
+    src = np.repeat(np.arange(n, dtype=np.int64), deg)
+    d64 = dst.astype(np.int64)
+    du, dv = deg[src], deg[d64]
+    own = (du > dv) | ((du == dv) & (src < d64))
+    b = lambda x: np.minimum(np.floor(np.log2(np.maximum(x, 1))).astype(np.int64), 23)
+    idx = b(du[own]) * 24 + b(dv[own])
+    return (np.bincount(idx, minlength=576), np.bincount(idx, weights=du[own].astype(np.float64), minlength=576),
+            np.bincount(idx, weights=dv[own].astype(np.float64), minlength=576))
+
+
+def test_bucket_stats_of_both_modes_after_relabel():
+    """Both modes' statistics come from one pass over the relabeled CSR: the
+    direct ones equal the original CSR's (degree buckets do not depend on the
+    numbering), the oriented ones are those of the relabeled CSR."""
+    G = accx.Graph.generate(accx.rmat_params(15, 16, seed=12))
+    off, dst = G.download()
+    G.relabel()
+    roff, rdst, _, _ = G.relabeled_csr()
+    for got, ref in ((G.bucket_stats(orient=False), _np_direct_stats(off, dst)),
+                     (G.bucket_stats(orient=True), _np_oriented_stats(roff, rdst))):
+        assert np.array_equal(got[0].astype(np.int64), ref[0])
+        assert np.array_equal(got[1], ref[1]) and np.array_equal(got[2], ref[2])
+    G.free()
+
+
 def test_oriented_model_table_is_argmin_and_counts_are_exact():
     from oracle import mlp_oracle
     m = accx.Model(seed=7)

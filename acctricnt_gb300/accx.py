@@ -90,17 +90,22 @@ class ServerStats(C.Structure):
 
 
 SCHED_NOFFSETS = 10
+# the bitmap-kind log2 offsets the scheduler tries (kOffsets in csrc/sched.cpp)
+SCHED_OFFSETS = (0.0, -0.5, -1.0, -1.5, -2.0, -3.0, -5.0, -64.0, 1.0, 64.0)
+SCHED_MAX_CANDIDATES = 8
 
 
 class SchedConfig(C.Structure):
-    _fields_ = [("seed", C.c_uint64), ("epochs", C.c_int), ("lr", C.c_float), ("reps", C.c_int), ("quick", C.c_int)]
+    _fields_ = [("seed", C.c_uint64), ("epochs", C.c_int), ("lr", C.c_float), ("reps", C.c_int), ("quick", C.c_int),
+                ("candidates", C.c_int)]
 
 
 class SchedInfo(C.Structure):
     _fields_ = [("rows", C.c_uint32 * 2), ("loss_initial", C.c_float * 2), ("loss_final", C.c_float * 2),
                 ("bitmap_offset", C.c_float * 2), ("calib_relative", (C.c_float * SCHED_NOFFSETS) * 2),
                 ("collect_s", C.c_double * 2), ("train_s", C.c_double * 2), ("calibrate_s", C.c_double * 2),
-                ("quick", C.c_int)]
+                ("quick", C.c_int), ("candidates", C.c_int * 2), ("chosen", C.c_int * 2),
+                ("candidate_score", (C.c_float * SCHED_MAX_CANDIDATES) * 2)]
 
 
 class SchedPlan(C.Structure):
@@ -614,9 +619,9 @@ class Scheduler:
         self._h = handle
 
     @classmethod
-    def train(cls, seed=1, epochs=0, lr=0.0, reps=0, quick=False):
+    def train(cls, seed=1, epochs=0, lr=0.0, reps=0, quick=False, candidates=0):
         h = C.c_void_p()
-        cfg = SchedConfig(int(seed), int(epochs), float(lr), int(reps), 1 if quick else 0)
+        cfg = SchedConfig(int(seed), int(epochs), float(lr), int(reps), 1 if quick else 0, int(candidates))
         _check(lib.accx_sched_train(C.byref(cfg), C.byref(h)), "sched_train")
         return cls(h)
 
@@ -655,7 +660,9 @@ class Scheduler:
                          "bitmap_offset": float(i.bitmap_offset[o]),
                          "calib_relative": [round(float(x), 4) for x in i.calib_relative[o]],
                          "collect_s": round(i.collect_s[o], 2), "train_s": round(i.train_s[o], 2),
-                         "calibrate_s": round(i.calibrate_s[o], 2)}
+                         "calibrate_s": round(i.calibrate_s[o], 2), "candidates": int(i.candidates[o]),
+                         "chosen": int(i.chosen[o]),
+                         "candidate_score": [round(float(x), 4) for x in i.candidate_score[o][:max(int(i.candidates[o]), 0)]]}
         out["quick"] = bool(i.quick)
         return out
 

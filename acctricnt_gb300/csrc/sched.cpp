@@ -13,10 +13,12 @@
 //     library's CUDA events (accx_bucket_timings);
 //   * each of the two models (direct and oriented kernels) is trained with the
 //     library's own FP16/FP32 training kernels on the rows of seven seeded
-//     graphs, then calibrated on whole counts: per-bucket timings taken alone
+//     graphs -- three candidates from different seeds on the same rows, since
+//     the per-bucket timings are noisy and a fit can extrapolate badly to large
+//     buckets -- then calibrated on whole counts: per-bucket timings taken alone
 //     overstate the bitmap kind (its owner staging serves all of an owner's
-//     buckets), so one log2 offset for that kind is chosen among ten
-//     candidates by the size-weighted count time on the calibration graphs;
+//     buckets), so the candidate and one log2 offset for that kind (among ten)
+//     are chosen by the size-weighted count time on the calibration graphs;
 //   * a plan attaches both models to a graph, predicts each mode's time from
 //     its own table and picks the faster mode; optionally it refines the
 //     chosen mode's offset on the graph itself by timing one whole count per
@@ -191,13 +193,17 @@ static int model_table(accx_model *m, accx_graph *g, int orient, uint8_t *t) {
   return orient ? accx_model_table_for_oriented(m, g, t) : accx_model_table_for(m, g, t);
 }
 
-// The bitmap kind's offset fitted on whole counts (see the file comment): score =
-// sum over graphs of weight x time / that graph's best candidate, weight = the
-// graph's share of the calibration set's CSR entries; ties keep the smaller offset.
-static int calibrate(accx_model *m, int orient, int quick, float *chosen, float *relative) {
+// The candidate model and the bitmap kind's offset fitted on whole counts (see
+// the file comment): every candidate's table at every offset is timed on each
+// calibration graph; score = sum over graphs of weight x time / that graph's
+// best time over all candidates and offsets, weight = the graph's share of the
+// calibration set's CSR entries.  The lowest score wins; ties keep the earlier
+// candidate and the smaller offset.  relative[] gets the winner's scores.
+static int calibrate(accx_model *const *ms, int K, int orient, int quick, int *chosen_model, float *chosen,
+                     float *relative, float *cand_score) {
   const std::vector<accx_gen_params> gs = calibration_graphs(quick);
-  const size_t G = gs.size();
-  std::vector<double> rel(G * ACCX_SCHED_NOFFSETS), w(G);
+  const size_t G = gs.size(), NO = ACCX_SCHED_NOFFSETS;
+  std::vector<double> t((size_t)K * G * NO), w(G);
   for (size_t gi = 0; gi < G; gi++) {
     accx_graph *g = nullptr;
     int rc = accx_graph_generate(&gs[gi], nullptr, &g);
@@ -207,36 +213,54 @@ static int calibrate(accx_model *m, int orient, int quick, float *chosen, float 
     uint64_t mm = 0;
     accx_graph_size(g, &n, &mm);
     w[gi] = (double)mm;
-    for (int c = 0; c < ACCX_SCHED_NOFFSETS && !rc; c++) {
-      uint8_t t[NBK];
-      rc = set_offset(m, kOffsets[c]);
-      if (!rc) rc = model_table(m, g, orient, t);
-      if (!rc) rc = table_count_ms(g, t, orient, quick ? 2 : 3, nullptr, &rel[gi * ACCX_SCHED_NOFFSETS + c]);
-    }
+    for (int k = 0; k < K && !rc; k++)
+      for (size_t c = 0; c < NO && !rc; c++) {
+        uint8_t tab[NBK];
+        rc = set_offset(ms[k], kOffsets[c]);
+        if (!rc) rc = model_table(ms[k], g, orient, tab);
+        if (!rc) rc = table_count_ms(g, tab, orient, quick ? 2 : 3, nullptr, &t[((size_t)k * G + gi) * NO + c]);
+      }
     accx_graph_free(g);
     if (rc) return rc;
   }
   double wsum = 0;
   for (double x : w) wsum += x;
-  double best = 0;
-  int bi = 0;
-  for (int c = 0; c < ACCX_SCHED_NOFFSETS; c++) {
-    double sc = 0;
-    for (size_t gi = 0; gi < G; gi++) {
-      double mn = rel[gi * ACCX_SCHED_NOFFSETS];
-      for (int d = 1; d < ACCX_SCHED_NOFFSETS; d++) mn = fmin(mn, rel[gi * ACCX_SCHED_NOFFSETS + d]);
-      sc += (wsum > 0 ? w[gi] / wsum : 0.0) * (mn > 0 ? rel[gi * ACCX_SCHED_NOFFSETS + c] / mn : 1.0);
-    }
-    relative[c] = (float)sc;
-    if (c == 0 || sc < best) {
-      best = sc;
-      bi = c;
-    }
+  std::vector<double> mn(G);
+  for (size_t gi = 0; gi < G; gi++) {
+    mn[gi] = t[gi * NO];
+    for (int k = 0; k < K; k++)
+      for (size_t c = 0; c < NO; c++) mn[gi] = fmin(mn[gi], t[((size_t)k * G + gi) * NO + c]);
   }
-  *chosen = kOffsets[bi];
-  return set_offset(m, kOffsets[bi]);
+  auto score = [&](int k, size_t c) {
+    double sc = 0;
+    for (size_t gi = 0; gi < G; gi++)
+      sc += (wsum > 0 ? w[gi] / wsum : 0.0) * (mn[gi] > 0 ? t[((size_t)k * G + gi) * NO + c] / mn[gi] : 1.0);
+    return sc;
+  };
+  double best = 0;
+  int bk = 0;
+  size_t bc = 0;
+  for (int k = 0; k < K; k++) {
+    double kb = 0;
+    for (size_t c = 0; c < NO; c++) {
+      const double sc = score(k, c);
+      if (c == 0 || sc < kb) kb = sc;
+      if ((k == 0 && c == 0) || sc < best) {
+        best = sc;
+        bk = k;
+        bc = c;
+      }
+    }
+    cand_score[k] = (float)kb;
+  }
+  for (size_t c = 0; c < NO; c++) relative[c] = (float)score(bk, c);
+  *chosen_model = bk;
+  *chosen = kOffsets[bc];
+  return set_offset(ms[bk], kOffsets[bc]);
 }
 
+// Training of one mode's model: rows collected once, K candidates trained on
+// them from different seeds, the calibration keeps one.
 static int train_one(accx_sched *s, int orient, const accx_sched_config &c) {
   auto t0 = clk::now();
   rows r;
@@ -247,20 +271,33 @@ static int train_one(accx_sched *s, int orient, const accx_sched_config &c) {
   if (r.k.empty()) return ACCX_ERR_NOT_READY;
   s->info.collect_s[orient] = secs_since(t0);
   s->info.rows[orient] = (uint32_t)r.k.size();
-  int rc = accx_model_create(c.seed, &s->model[orient]);
-  if (rc) return rc;
-  accx_model *m = s->model[orient];
+  const int K = c.candidates;
+  std::vector<accx_model *> ms(K, nullptr);
+  std::vector<float> l0(K), l1(K);
+  int rc = ACCX_OK;
   t0 = clk::now();
-  rc = accx_model_loss_grad(m, r.x.data(), r.k.data(), r.y.data(), (uint32_t)r.k.size(), nullptr,
-                            &s->info.loss_initial[orient]);
-  if (!rc) rc = accx_model_train(m, r.x.data(), r.k.data(), r.y.data(), (uint32_t)r.k.size(), c.epochs, c.lr,
-                                 &s->info.loss_final[orient]);
-  if (rc) return rc;
+  for (int k = 0; k < K && !rc; k++) {
+    rc = accx_model_create(c.seed + (uint64_t)k, &ms[k]);
+    if (!rc) rc = accx_model_loss_grad(ms[k], r.x.data(), r.k.data(), r.y.data(), (uint32_t)r.k.size(), nullptr, &l0[k]);
+    if (!rc) rc = accx_model_train(ms[k], r.x.data(), r.k.data(), r.y.data(), (uint32_t)r.k.size(), c.epochs, c.lr, &l1[k]);
+  }
   s->info.train_s[orient] = secs_since(t0);
-  t0 = clk::now();
-  rc = calibrate(m, orient, c.quick, &s->info.bitmap_offset[orient], s->info.calib_relative[orient]);
-  s->info.calibrate_s[orient] = secs_since(t0);
-  return rc;
+  int ck = 0;
+  if (!rc) {
+    t0 = clk::now();
+    rc = calibrate(ms.data(), K, orient, c.quick, &ck, &s->info.bitmap_offset[orient], s->info.calib_relative[orient],
+                   s->info.candidate_score[orient]);
+    s->info.calibrate_s[orient] = secs_since(t0);
+  }
+  for (int k = 0; k < K; k++)
+    if (ms[k] && (rc || k != ck)) accx_model_free(ms[k]);
+  if (rc) return rc;
+  s->model[orient] = ms[ck];
+  s->info.candidates[orient] = K;
+  s->info.chosen[orient] = ck;
+  s->info.loss_initial[orient] = l0[ck];
+  s->info.loss_final[orient] = l1[ck];
+  return ACCX_OK;
 }
 
 extern "C" int accx_sched_train(const accx_sched_config *cfg, accx_sched **out) {
@@ -272,6 +309,8 @@ extern "C" int accx_sched_train(const accx_sched_config *cfg, accx_sched **out) 
   if (c.epochs <= 0) c.epochs = c.quick ? 800 : 4000;
   if (!(c.lr > 0)) c.lr = 3e-3f;
   if (c.reps <= 0) c.reps = 2;
+  if (c.candidates <= 0) c.candidates = c.quick ? 1 : 3;
+  if (c.candidates > ACCX_SCHED_MAX_CANDIDATES) return ACCX_ERR_INVALID_ARG;
   accx_sched *s = new (std::nothrow) accx_sched();
   if (!s) return ACCX_ERR_OOM;
   s->info.quick = c.quick;
@@ -306,14 +345,16 @@ extern "C" int accx_sched_get_info(const accx_sched *s, accx_sched_info *info) {
   return ACCX_OK;
 }
 
-// File: text, "accx-sched 1", then per model (direct, then oriented) a line
+// File: text, "accx-sched 2", then per model (direct, then oriented) a line
 // "model <orient> <kind bias x3>", a line of ACCX_MODEL_NPARAMS parameters and an
-// info line; floats in %.9g (round trip exact for FP32).
+// info line (version 2 ends it with the candidates, the one kept and
+// ACCX_SCHED_MAX_CANDIDATES scores; version 1 files, without them, still load);
+// floats in %.9g (round trip exact for FP32).
 extern "C" int accx_sched_save(const accx_sched *s, const char *path) {
   if (!s || !path || !s->model[0] || !s->model[1]) return ACCX_ERR_INVALID_ARG;
   FILE *f = fopen(path, "w");
   if (!f) return ACCX_ERR_IO;
-  fprintf(f, "accx-sched 1\n");
+  fprintf(f, "accx-sched 2\n");
   for (int o = 0; o < 2; o++) {
     float b[ACCX_MODEL_OUT], p[ACCX_MODEL_NPARAMS];
     int rc = accx_model_get_kind_bias(s->model[o], b);
@@ -328,6 +369,8 @@ extern "C" int accx_sched_save(const accx_sched *s, const char *path) {
     fprintf(f, "info %u %.9g %.9g %.9g %.6f %.6f %.6f %d", in.rows[o], in.loss_initial[o], in.loss_final[o],
             in.bitmap_offset[o], in.collect_s[o], in.train_s[o], in.calibrate_s[o], in.quick);
     for (int c = 0; c < ACCX_SCHED_NOFFSETS; c++) fprintf(f, " %.9g", in.calib_relative[o][c]);
+    fprintf(f, " %d %d", in.candidates[o], in.chosen[o]);
+    for (int k = 0; k < ACCX_SCHED_MAX_CANDIDATES; k++) fprintf(f, " %.9g", in.candidate_score[o][k]);
     fprintf(f, "\n");
   }
   const bool ok = !ferror(f);
@@ -344,7 +387,7 @@ extern "C" int accx_sched_load(const char *path, accx_sched **out) {
     return ACCX_ERR_OOM;
   }
   int rc = ACCX_OK, ver = 0;
-  if (fscanf(f, " accx-sched %d", &ver) != 1 || ver != 1) rc = ACCX_ERR_IO;
+  if (fscanf(f, " accx-sched %d", &ver) != 1 || (ver != 1 && ver != 2)) rc = ACCX_ERR_IO;
   for (int o = 0; o < 2 && !rc; o++) {
     int oo = -1;
     float b[ACCX_MODEL_OUT], p[ACCX_MODEL_NPARAMS];
@@ -360,6 +403,11 @@ extern "C" int accx_sched_load(const char *path, accx_sched **out) {
       rc = ACCX_ERR_IO;
     for (int c = 0; c < ACCX_SCHED_NOFFSETS && !rc; c++)
       if (fscanf(f, " %f", &in.calib_relative[o][c]) != 1) rc = ACCX_ERR_IO;
+    if (!rc && ver >= 2) {  // version 2 adds the candidates record
+      if (fscanf(f, " %d %d", &in.candidates[o], &in.chosen[o]) != 2) rc = ACCX_ERR_IO;
+      for (int k = 0; k < ACCX_SCHED_MAX_CANDIDATES && !rc; k++)
+        if (fscanf(f, " %f", &in.candidate_score[o][k]) != 1) rc = ACCX_ERR_IO;
+    }
     if (!rc) rc = accx_model_create(1, &s->model[o]);
     if (!rc) rc = accx_model_set_params(s->model[o], p);
     if (!rc) rc = accx_model_set_kind_bias(s->model[o], b);

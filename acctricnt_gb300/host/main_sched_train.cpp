@@ -27,9 +27,10 @@ int main(int argc, char *argv[]) {
   accx_sched_info in;
   accx_sched_get_info(s, &in);
   for (int o = 0; o < 2; o++)
-    printf("%s model: %u rows, loss %.3f -> %.3f, bitmap offset %.2f (collect %.1f s, train %.1f s, calibrate %.1f s)\n",
-           o ? "oriented" : "direct", in.rows[o], in.loss_initial[o], in.loss_final[o], in.bitmap_offset[o],
-           in.collect_s[o], in.train_s[o], in.calibrate_s[o]);
+    printf("%s model: %u rows, candidate %d of %d, loss %.3f -> %.3f, bitmap offset %.2f (collect %.1f s, train %.1f s, "
+           "calibrate %.1f s)\n",
+           o ? "oriented" : "direct", in.rows[o], in.chosen[o] + 1, in.candidates[o], in.loss_initial[o],
+           in.loss_final[o], in.bitmap_offset[o], in.collect_s[o], in.train_s[o], in.calibrate_s[o]);
   printf("wrote %s\n", argv[1]);
   accx_sched_free(s);
   return 0;

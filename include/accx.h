@@ -329,7 +329,11 @@ typedef struct {
   float lr;       /* learning rate (0 = 3e-3) */
   int reps;       /* timing repetitions per bucket and kind (0 = 2) */
   int quick;      /* 1: four small training graphs, also used for calibration (tests) */
+  int candidates; /* models trained per mode (seeds seed, seed+1, ...) on the same rows; the
+                     calibration keeps the best (0 = 3; 1 when quick; at most
+                     ACCX_SCHED_MAX_CANDIDATES) */
 } accx_sched_config;
+#define ACCX_SCHED_MAX_CANDIDATES 8
 typedef struct {
   uint32_t rows[2];                   /* training rows per model (0 direct, 1 oriented) */
   float loss_initial[2], loss_final[2];
@@ -337,6 +341,10 @@ typedef struct {
   float calib_relative[2][ACCX_SCHED_NOFFSETS];  /* size-weighted relative count time per offset */
   double collect_s[2], train_s[2], calibrate_s[2];
   int quick;
+  int candidates[2];                  /* models trained per mode */
+  int chosen[2];                      /* the candidate kept */
+  float candidate_score[2][ACCX_SCHED_MAX_CANDIDATES];  /* each one's best calibration score
+                                                           (relative to the best count per graph) */
 } accx_sched_info;
 typedef struct {
   int orient;                 /* the chosen mode */
@@ -351,8 +359,9 @@ typedef struct {
 } accx_sched_plan;
 
 /* Trains both models on the device: per-bucket timings of seven seeded graphs
- * (relabeled), Adam training with the library's kernels, then the bitmap
- * offset calibrated on whole counts of those graphs plus R-MAT 20 and 22.
+ * (relabeled), Adam training with the library's kernels of several candidate
+ * models (different seeds, the same rows), then the candidate and its bitmap
+ * offset chosen on whole counts of those graphs plus R-MAT 20 and 22.
  * Takes tens of seconds on a GB300 (a few with quick = 1).  cfg NULL = defaults. */
 int accx_sched_train(const accx_sched_config *cfg, accx_sched **out);
 int accx_sched_free(accx_sched *s);

@@ -83,11 +83,12 @@ FIXED = {"direct_heuristic": dict(policy="heuristic"), "direct_merge": dict(poli
 def test_scheduler_file_round_trip_and_plan(quick_sched_file, tmp_path):
     S = accx.Scheduler.load(quick_sched_file)
     with open(quick_sched_file) as f:
-        assert f.readline().startswith("accx-sched 1")
+        assert f.readline().startswith("accx-sched 2")
     info = S.info()
     assert info["quick"]
     for mode in ("direct", "oriented"):
         assert info[mode]["rows"] > 0 and info[mode]["loss_final"] < info[mode]["loss_initial"]
+        assert info[mode]["candidates"] == 1 and info[mode]["chosen"] == 0
     p2 = str(tmp_path / "again.model")
     S.save(p2)
     T = accx.Scheduler.load(p2)
@@ -104,6 +105,37 @@ def test_scheduler_file_round_trip_and_plan(quick_sched_file, tmp_path):
         assert np.array_equal(G.count(policy="model", orient=o), ref)
     with pytest.raises(accx.AccxError):
         accx.Scheduler.load(str(tmp_path / "missing.model"))
+
+
+def test_version1_scheduler_files_still_load(quick_sched_file, tmp_path):
+    """A version-1 file (no candidates record on the info lines) loads with the
+    same models."""
+    lines = open(quick_sched_file).read().splitlines()
+    out = ["accx-sched 1"]
+    for ln in lines[1:]:
+        if ln.startswith("info "):
+            ln = " ".join(ln.split()[:9 + accx.SCHED_NOFFSETS])
+        out.append(ln)
+    p1 = str(tmp_path / "v1.model")
+    open(p1, "w").write("\n".join(out) + "\n")
+    S, T = accx.Scheduler.load(quick_sched_file), accx.Scheduler.load(p1)
+    for o in (False, True):
+        assert np.array_equal(S.model(o).params(), T.model(o).params())
+        assert np.array_equal(S.model(o).kind_bias(), T.model(o).kind_bias())
+    assert T.info()["direct"]["candidates"] == 0
+
+
+def test_full_training_keeps_the_best_scoring_candidate(default_sched):
+    """The full scheduler trains three candidates per mode and keeps the one
+    with the lowest whole-count calibration score, at its best offset."""
+    info = default_sched.info()
+    for mode in ("direct", "oriented"):
+        d = info[mode]
+        assert d["candidates"] == 3 and 0 <= d["chosen"] < 3
+        sc = d["candidate_score"]
+        assert len(sc) == 3 and sc[d["chosen"]] == min(sc) and sc[d["chosen"]] >= 1.0
+        assert abs(min(d["calib_relative"]) - sc[d["chosen"]]) < 1e-6
+        assert d["calib_relative"][accx.SCHED_OFFSETS.index(d["bitmap_offset"])] == min(d["calib_relative"])
 
 
 def test_plan_tuning_keeps_a_candidate_and_counts_stay_exact(quick_sched_file):

@@ -262,31 +262,23 @@ struct bs_run {
   }
 };
 
-// CTAs loop over tiles of NT*BS_EPT entries and reach the device counters once.
+// Threads take chunks of BS_EPT consecutive entries (grid-stride); a chunk lies
+// in one 256-entry tile, whose first and last rows tilerow[] holds, so a thread
+// finds its row without the CTA (no barrier per tile).  The CTA's histograms
+// reach the device counters once.
 template <int NT>
-__global__ void __launch_bounds__(NT) k_bucket_stats(const uint32_t *__restrict__ off, const uint32_t *__restrict__ tilerow,
-                                                     const int32_t *__restrict__ dst, uint32_t n, uint32_t m,
-                                                     const uint32_t *__restrict__ pre,
-                                                     unsigned long long *__restrict__ st_direct,
-                                                     unsigned long long *__restrict__ st_orient) {
-  static_assert((NT * BS_EPT) % 256 == 0, "tiles of whole tile-row tiles");
+__global__ void __launch_bounds__(NT, 5) k_bucket_stats(const uint32_t *__restrict__ off, const uint32_t *__restrict__ tilerow,
+                                                        const int32_t *__restrict__ dst, uint32_t n, uint32_t m,
+                                                        const uint32_t *__restrict__ pre,
+                                                        unsigned long long *__restrict__ st_direct,
+                                                        unsigned long long *__restrict__ st_orient) {
+  static_assert(256 % BS_EPT == 0, "chunks inside tile-row tiles");
   __shared__ unsigned long long hs[2][3 * NBB];
-  __shared__ uint32_t s_lo, s_hi;
   for (int i = threadIdx.x; i < 6 * NBB; i += NT) (&hs[0][0])[i] = 0;
-  const uint32_t span = NT * BS_EPT;
-  const uint32_t ntiles = (uint32_t)(((unsigned long long)m + span - 1) / span);
-  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const uint32_t base = t * span;
-    __syncthreads();  // the histograms' clearing, and the last tile's row range read
-    if (threadIdx.x == 0) {
-      // tilerow[k] = the row of entry 256k, its last element the row of entry m-1
-      const uint32_t last = (base + span < m ? base + span : m) - 1;
-      s_lo = __ldg(tilerow + base / 256u);
-      s_hi = __ldg(tilerow + last / 256u + 1u);
-    }
-    __syncthreads();
-    const uint32_t e0 = base + threadIdx.x * BS_EPT;
-    if (e0 >= m) continue;
+  __syncthreads();
+  const uint32_t nchunks = (uint32_t)(((unsigned long long)m + BS_EPT - 1) / BS_EPT);
+  for (uint32_t ch = blockIdx.x * NT + threadIdx.x; ch < nchunks; ch += gridDim.x * NT) {
+    const uint32_t e0 = ch * BS_EPT;
     const uint32_t e1 = e0 + BS_EPT < m ? e0 + BS_EPT : m;
     // the partners' sizes first (independent loads in flight), then the rows
     uint32_t vv[BS_EPT], dd[BS_EPT], pp[BS_EPT];
@@ -297,7 +289,9 @@ __global__ void __launch_bounds__(NT) k_bucket_stats(const uint32_t *__restrict_
       dd[j] = __ldg(off + vv[j] + 1) - __ldg(off + vv[j]);
       pp[j] = __ldg(pre + vv[j]);
     }
-    uint32_t u = accx_row_of(off, s_lo, s_hi + 1, e0);
+    // tilerow[k] = the row of entry 256k, its last element the row of entry m-1
+    const uint32_t t = e0 / 256u;
+    uint32_t u = accx_row_of(off, __ldg(tilerow + t), __ldg(tilerow + t + 1) + 1, e0);
     uint32_t rb = __ldg(off + u), re = __ldg(off + u + 1), pu = __ldg(pre + u);
     bs_run rd, ro;
 #pragma unroll
@@ -404,7 +398,7 @@ static int ensure_features(accx_graph *g, cudaStream_t s, int mode) {
       tilerow = rel ? g->d_rtilerow : g->d_tilerow;
     }
     const uint32_t tiles = (uint32_t)(((unsigned long long)m + 256 * BS_EPT - 1) / (256 * BS_EPT));
-    const uint32_t grid = std::min(tiles, (uint32_t)accx_sm_count(g->device) * 4);
+    const uint32_t grid = std::min(tiles, (uint32_t)accx_sm_count(g->device) * 5);
     k_bucket_stats<256><<<grid, 256, 0, s>>>(off, tilerow, rel ? g->d_rdst : g->d_dst, g->n, m, g->d_pre,
                                              st->d_stats[0], st->d_stats[1]);
   }

@@ -456,3 +456,4 @@ __global__ void k_combine_or(uint32_t m, const uint32_t *__restrict__ rev, int32
   const uint32_t r = rev[e];
   if (r != 0xffffffffu && r > e) cnt[e] = cnt[r];
 }
+

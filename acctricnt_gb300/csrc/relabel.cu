@@ -139,10 +139,22 @@ __global__ void k_put_range(const uint32_t *__restrict__ key, const uint32_t *__
     relabel_put(p, key[p], val[p], rdst, map);
 }
 
+// Four entries per thread and step, their index loads and then their gathers
+// issued together: the gathers are random reads, bound by latency at one a thread.
 __global__ void k_gather_counts(const int32_t *__restrict__ cnt_r, const uint32_t *__restrict__ map, uint32_t m,
                                 int32_t *__restrict__ cnt) {
-  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < m; e += gridDim.x * blockDim.x)
-    cnt[e] = __ldg(cnt_r + __ldg(map + e));
+  const uint32_t stride = gridDim.x * blockDim.x;
+  uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+  for (; e + 3 * stride < m; e += 4 * stride) {
+    const uint32_t a = __ldg(map + e), b = __ldg(map + e + stride), c = __ldg(map + e + 2 * stride),
+                   d = __ldg(map + e + 3 * stride);
+    const int32_t x = __ldg(cnt_r + a), y = __ldg(cnt_r + b), z = __ldg(cnt_r + c), w = __ldg(cnt_r + d);
+    cnt[e] = x;
+    cnt[e + stride] = y;
+    cnt[e + 2 * stride] = z;
+    cnt[e + 3 * stride] = w;
+  }
+  for (; e < m; e += stride) cnt[e] = __ldg(cnt_r + __ldg(map + e));
 }
 
 int accx_relabel_gather(accx_graph *g, cudaStream_t s) {

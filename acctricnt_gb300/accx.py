@@ -17,6 +17,7 @@ ERR_INVALID_ARG, ERR_CUDA, ERR_OOM, ERR_SELF_LOOP, ERR_UNSORTED, ERR_RANGE, ERR_
     ERR_TOO_LARGE, ERR_NOT_READY, ERR_TIMEOUT, ERR_ADMISSION, ERR_NO_DEVICE = range(-1, -14, -1)
 
 GRAPH_VALIDATE = 1
+GRAPH_VALIDATE_EXACT = 2
 GEN_RMAT, GEN_ER, GEN_CHUNG_LU = 0, 1, 2
 KIND_MERGE, KIND_GALLOP, KIND_BITMAP = 0, 1, 2
 KIND_NAMES = ("merge", "gallop", "bitmap")
@@ -29,6 +30,12 @@ MODEL_IN, MODEL_H, MODEL_OUT = 8, 32, 3
 MODEL_NPARAMS = MODEL_IN * MODEL_H + MODEL_H + MODEL_H * MODEL_H + MODEL_H + MODEL_H * MODEL_OUT + MODEL_OUT
 PHASES = ("plan", "merge", "gallop", "bitmap", "mirror")
 UNCLASSIFIED, CORE, HUB = 0, 1, 2
+
+
+def _validate_flags(validate):
+    if validate == "exact":
+        return GRAPH_VALIDATE | GRAPH_VALIDATE_EXACT
+    return GRAPH_VALIDATE if validate else 0
 
 
 class AccxError(RuntimeError):
@@ -307,11 +314,12 @@ class Graph:
 
     @classmethod
     def from_csr(cls, off, dst, validate=True, stream=None):
+        """validate: True (symmetry by fingerprints), "exact" (by the sort) or False."""
         off = np.ascontiguousarray(off, np.uint32)
         dst = np.ascontiguousarray(dst, np.int32)
         h = C.c_void_p()
         _check(lib.accx_graph_create(_ptr(off), _ptr(dst) if len(dst) else None, len(off) - 1, len(dst),
-                                     GRAPH_VALIDATE if validate else 0, _stream_ptr(stream), C.byref(h)),
+                                     _validate_flags(validate), _stream_ptr(stream), C.byref(h)),
                "graph_create")
         return cls(h)
 
@@ -319,14 +327,14 @@ class Graph:
     def from_device(cls, off_ptr, dst_ptr, n, m, validate=True, stream=None):
         h = C.c_void_p()
         _check(lib.accx_graph_create(C.c_void_p(off_ptr), C.c_void_p(dst_ptr), n, m,
-                                     GRAPH_VALIDATE if validate else 0, _stream_ptr(stream), C.byref(h)),
+                                     _validate_flags(validate), _stream_ptr(stream), C.byref(h)),
                "graph_create")
         return cls(h)
 
     @classmethod
     def load_dir(cls, path, validate=True, stream=None):
         h = C.c_void_p()
-        _check(lib.accx_graph_load_dir(path.encode(), GRAPH_VALIDATE if validate else 0, _stream_ptr(stream),
+        _check(lib.accx_graph_load_dir(path.encode(), _validate_flags(validate), _stream_ptr(stream),
                                        C.byref(h)), "graph_load_dir")
         return cls(h)
 

@@ -125,7 +125,7 @@ int accx_grid_for(int device, int block, int per_sm);
 int accx_sm_count(int device);
 
 // Internal: creates a handle around device arrays already owned by it.
-int accx_graph_validate_device(accx_graph *g, int full, cudaStream_t s);
+int accx_graph_validate_device(accx_graph *g, int full, int exact, cudaStream_t s);
 int accx_ensure_count_scratch(accx_graph *g);
 // Prefix lengths (neighbours with smaller ids) of the CSR counts run on (the
 // relabeled copy when there is one) into g->d_pre (count.cu).

@@ -205,11 +205,31 @@ int accx_grid_for(int device, int block, int per_sm) {
 // non-searching entry; distinct entries have distinct reverses in sorted lists
 // without repeats) and they are exactly half of all entries, the reverse map is a
 // bijection onto the other half: the graph is symmetric.
+// Symmetry fingerprints: two published 64-bit finalisers (SplitMix64's, and
+// MurmurHash3's fmix64 applied to the key plus an odd constant) of the key
+// (a << 32 | b).  Over all entries, sum of f(u,v) - f(v,u) is zero (mod 2^64) on
+// a symmetric graph.
+__device__ __forceinline__ unsigned long long fp_splitmix(unsigned long long z) {
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ unsigned long long fp_fmix(unsigned long long k) {
+  k += 0x9e3779b97f4a7c15ull;
+  k ^= k >> 33;
+  k *= 0xff51afd7ed558ccdull;
+  k ^= k >> 33;
+  k *= 0xc4ceb9fe1a85ec53ull;
+  return k ^ (k >> 33);
+}
+#define FP_SLOTS 64  // fingerprint accumulators (CTAs spread their atomics over them)
+
 template <bool SEARCH>
 __global__ void k_validate(const uint32_t *__restrict__ off, const uint32_t *__restrict__ tilerow, const int32_t *__restrict__ dst, uint32_t n,
                            uint32_t m, int full, int *__restrict__ status, unsigned long long *__restrict__ searched,
-                           uint32_t *__restrict__ rev) {
+                           uint32_t *__restrict__ rev, unsigned long long *__restrict__ fp) {
   __shared__ accx_tile_rows<256> sh;
+  __shared__ unsigned long long s_fp[2][8];
   uint32_t base = blockIdx.x * 256u;
   uint32_t e = base + threadIdx.x;
   uint32_t u = accx_tile_row<256>(off, tilerow, n, m, base, e, &sh);
@@ -243,6 +263,30 @@ __global__ void k_validate(const uint32_t *__restrict__ off, const uint32_t *__r
   if (SEARCH && full) {  // uniform over the block
     const int c = __syncthreads_count(chk);
     if (threadIdx.x == 0 && c) atomicAdd(searched, (unsigned long long)c);
+  }
+  if (fp) {  // uniform over the grid: the fingerprints of this block's entries
+    unsigned long long d1 = 0, d2 = 0;
+    if (e < m && !flag) {
+      const unsigned long long v = (uint32_t)dst[e];
+      const unsigned long long a = ((unsigned long long)u << 32) | v, b = (v << 32) | u;
+      d1 = fp_splitmix(a) - fp_splitmix(b);
+      d2 = fp_fmix(a) - fp_fmix(b);
+    }
+#pragma unroll
+    for (int d = 16; d >= 1; d >>= 1) {
+      d1 += __shfl_xor_sync(ACCX_FULL_MASK, d1, d);
+      d2 += __shfl_xor_sync(ACCX_FULL_MASK, d2, d);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      s_fp[0][threadIdx.x >> 5] = d1;
+      s_fp[1][threadIdx.x >> 5] = d2;
+    }
+    __syncthreads();
+    if (threadIdx.x < 2) {
+      unsigned long long t = 0;
+      for (int w = 0; w < 8; w++) t += s_fp[threadIdx.x][w];
+      if (t) atomicAdd(&fp[threadIdx.x * FP_SLOTS + blockIdx.x % FP_SLOTS], t);  // wraps mod 2^64
+    }
   }
 }
 
@@ -366,26 +410,46 @@ __global__ void k_check_offsets(const uint32_t *__restrict__ off, uint32_t n, ui
   if (blockIdx.x == 0 && threadIdx.x == 0 && (off[0] != 0 || off[n] != m)) atomicOr(status, V_RANGE);
 }
 
-int accx_graph_validate_device(accx_graph *g, int full, cudaStream_t s) {
-  int *d_status = nullptr;  // [0] defect bits, [2..3] searched-entry count (8-byte aligned)
-  ACCX_CUDA_TRY(cudaMalloc(&d_status, 4 * sizeof(int)));
+// full: the order, self-loop and symmetry checks besides the range checks;
+// exact: symmetry by the sort (accx_rev_by_sort, which also records the reverse
+// index) instead of the fingerprints.
+int accx_graph_validate_device(accx_graph *g, int full, int exact, cudaStream_t s) {
+  // [0] defect bits, [2..3] searched-entry count, then 2 x FP_SLOTS fingerprint sums
+  const size_t words = 4 + 4 * FP_SLOTS;
+  int *d_status = nullptr;
+  ACCX_CUDA_TRY(cudaMalloc(&d_status, words * sizeof(int)));
   unsigned long long *d_searched = reinterpret_cast<unsigned long long *>(d_status + 2);
+  unsigned long long *d_fp = reinterpret_cast<unsigned long long *>(d_status + 4);
   int rc = ACCX_OK;
   do {
-    if (cudaMemsetAsync(d_status, 0, 4 * sizeof(int), s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
+    if (cudaMemsetAsync(d_status, 0, words * sizeof(int), s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
     k_check_offsets<<<accx_grid_for(g->device, 256, 4), 256, 0, s>>>(g->d_off, g->n, (uint32_t)g->m, d_status);
     int st = 0;
     if (cudaMemcpyAsync(&st, d_status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
     if (st) { rc = ACCX_ERR_RANGE; break; }
     if ((rc = accx_tilerow_build(g, g->d_off, &g->d_tilerow, s)) != ACCX_OK) break;
-    if (!g->m) break;
+    if (!g->m) {
+      if (full) g->symmetric = true;
+      break;
+    }
     const uint32_t blocks = (uint32_t)((g->m + 255) / 256);
+    const bool fingerprints = full && !exact;
     k_validate<false><<<blocks, 256, 0, s>>>(g->d_off, g->d_tilerow, g->d_dst, g->n, (uint32_t)g->m, full, d_status,
-                                             nullptr, nullptr);
+                                             nullptr, nullptr, fingerprints ? d_fp : nullptr);
+    unsigned long long fp[2 * FP_SLOTS];
     if (cudaMemcpyAsync(&st, d_status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        (fingerprints && cudaMemcpyAsync(fp, d_fp, sizeof(fp), cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
         cudaStreamSynchronize(s) != cudaSuccess) { rc = ACCX_ERR_CUDA; break; }
-    if (full && !st) {
+    if (fingerprints && !st) {
+      unsigned long long f1 = 0, f2 = 0;
+      for (int i = 0; i < FP_SLOTS; i++) {
+        f1 += fp[i];
+        f2 += fp[FP_SLOTS + i];
+      }
+      if (f1 || f2) st = V_ASYM;
+    }
+    if (full && exact && !st) {
       // symmetry, and with it the reverse index, by the sort; by a search per
       // entry pair when its scratch does not fit
       uint32_t *rev = nullptr;
@@ -397,7 +461,7 @@ int accx_graph_validate_device(accx_graph *g, int full, cudaStream_t s) {
           rev = nullptr;  // no room: counts build the index themselves
         }
         k_validate<true><<<blocks, 256, 0, s>>>(g->d_off, g->d_tilerow, g->d_dst, g->n, (uint32_t)g->m, full, d_status,
-                                                d_searched, rev);
+                                                d_searched, rev, nullptr);
         unsigned long long searched = 0;
         if (cudaMemcpyAsync(&st, d_status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
             cudaMemcpyAsync(&searched, d_searched, sizeof(searched), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
@@ -421,8 +485,8 @@ int accx_graph_validate_device(accx_graph *g, int full, cudaStream_t s) {
         if (!st) g->d_rev_orig = rev;  // complete only for a graph that passed
         else accx_dev_free(rev, nullptr);
       }
-      if (!st) g->symmetric = true;
     }
+    if (full && !st) g->symmetric = true;
     rc = (st & V_RANGE) ? ACCX_ERR_RANGE : (st & V_SELF) ? ACCX_ERR_SELF_LOOP
        : (st & V_UNSORTED) ? ACCX_ERR_UNSORTED : (st & V_ASYM) ? ACCX_ERR_ASYMMETRIC : ACCX_OK;
   } while (0);
@@ -472,7 +536,8 @@ extern "C" int accx_graph_create(const uint32_t *off, const int32_t *dst, uint32
   if (rc) return rc;
   rc = accx_copy_in(g->d_off, off, sizeof(uint32_t) * ((size_t)n + 1), s);
   if (!rc) rc = accx_copy_in(g->d_dst, dst, sizeof(int32_t) * (size_t)m, s);
-  if (!rc) rc = accx_graph_validate_device(g, (flags & ACCX_GRAPH_VALIDATE) ? 1 : 0, s);
+  if (!rc) rc = accx_graph_validate_device(g, (flags & ACCX_GRAPH_VALIDATE) ? 1 : 0,
+                                           (flags & ACCX_GRAPH_VALIDATE_EXACT) ? 1 : 0, s);
   if (!rc) {
     cudaError_t e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) { accx_set_cuda_error(e, "create", __FILE__, __LINE__); rc = ACCX_ERR_CUDA; }

@@ -60,6 +60,14 @@ typedef struct accx_graph accx_graph;
 
 /* Flags for accx_graph_create. */
 #define ACCX_GRAPH_VALIDATE 1u       /* check self loops, order, range, symmetry on the GPU */
+/* With ACCX_GRAPH_VALIDATE, how symmetry is checked.  By default in the same pass
+ * as the other checks, by two 64-bit multiset fingerprints (the sums over all
+ * entries (u,v) of two mixing functions of (u,v), against the same sums of (v,u));
+ * rows are already checked strictly increasing, so an asymmetric graph passes
+ * only if both 64-bit sums collide.  ACCX_GRAPH_VALIDATE_EXACT instead sorts the
+ * entries by neighbour id (about 16 bytes per entry of scratch, several times the
+ * time) and records the reverse index on the way. */
+#define ACCX_GRAPH_VALIDATE_EXACT 2u
 
 /* Copies a CSR (off[n+1], dst[m], host or device pointers -- detected with
  * cudaPointerGetAttributes) to device memory and returns a handle.  dst holds

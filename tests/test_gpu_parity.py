@@ -255,8 +255,9 @@ def test_rmat24_full_parity_with_oracle():
     G.free()
 
 
+@pytest.mark.parametrize("mode", [True, "exact"])
 @pytest.mark.parametrize("bad", ["self_loop", "unsorted", "asymmetric", "range"])
-def test_invalid_graphs_rejected(bad):
+def test_invalid_graphs_rejected(bad, mode):
     off = np.array([0, 2, 4, 6], np.uint32)
     dst = np.array([1, 2, 0, 2, 0, 1], np.int32)
     code = {"self_loop": accx.ERR_SELF_LOOP, "unsorted": accx.ERR_UNSORTED, "asymmetric": accx.ERR_ASYMMETRIC,
@@ -271,29 +272,45 @@ def test_invalid_graphs_rejected(bad):
     else:
         dst = np.array([1, 9, 0, 2, 0, 1], np.int32)
     with pytest.raises(accx.AccxError) as ei:
-        accx.Graph.from_csr(off, dst)
+        accx.Graph.from_csr(off, dst, validate=mode)
     assert ei.value.status == code
 
 
-@pytest.mark.parametrize("case", ["directed_cycle", "swapped_targets"])
-def test_asymmetric_graphs_with_balanced_degrees_rejected(case):
+@pytest.mark.parametrize("mode", [True, "exact"])
+@pytest.mark.parametrize("case", ["directed_cycle", "swapped_targets", "one_edge_moved"])
+def test_asymmetric_graphs_with_balanced_degrees_rejected(case, mode):
     """Every vertex is a neighbour as often as its own list is long, yet the
-    graph is not symmetric: the row-of-neighbour test of the sorted check (not
-    the degree test) has to catch these."""
+    graph is not symmetric: in the exact check the row-of-neighbour test of the
+    sorted entries (not the degree test) has to catch these; the fingerprints
+    catch them too."""
     if case == "directed_cycle":
         off, dst = np.array([0, 1, 2, 3], np.uint32), np.array([1, 2, 0], np.int32)
-    else:  # the edges 0-1 and 2-3 with one target of each pair swapped
+    elif case == "swapped_targets":  # the edges 0-1 and 2-3 with one target of each pair swapped
         off, dst = np.array([0, 1, 2, 3, 4], np.uint32), np.array([3, 0, 1, 2], np.int32)
+    else:  # a large symmetric graph with one entry's target moved (rows stay sorted)
+        off, dst = accx.generate_host(accx.rmat_params(16, 16, seed=3))
+        dst = dst.copy()
+        deg = np.diff(off.astype(np.int64))
+        u = int(np.nonzero(deg >= 3)[0][len(np.nonzero(deg >= 3)[0]) // 2])
+        row = dst[off[u]:off[u + 1]]
+        lo, hi = int(row[0]), int(row[1])
+        assert hi - lo >= 1
+        w = next((x for x in range(lo + 1, hi) if x != u), None)
+        if w is None:  # the first gap of the row between two consecutive targets
+            i = next(i for i in range(len(row) - 1) if row[i + 1] - row[i] > 1 and row[i] + 1 != u)
+            dst[off[u] + i] = row[i] + 1
+        else:
+            dst[off[u]] = w
     with pytest.raises(accx.AccxError) as ei:
-        accx.Graph.from_csr(off, dst)
+        accx.Graph.from_csr(off, dst, validate=mode)
     assert ei.value.status == accx.ERR_ASYMMETRIC
 
 
-@pytest.mark.parametrize("validate", [True, False])
+@pytest.mark.parametrize("validate", [True, "exact", False])
 def test_reverse_index_sources_give_the_same_counts(validate):
-    """The oriented count's reverse index comes from validation (validated
-    handle, original CSR), from the sort (relabeled CSR of a known-symmetric
-    handle) or from the search (an unvalidated handle): the same counts."""
+    """The oriented count's reverse index comes from exact validation (original
+    CSR), from the sort (a known-symmetric handle: validated or generated) or
+    from the search (an unvalidated handle): the same counts."""
     off, dst = accx.generate_host(accx.rmat_params(14, 16, seed=8))
     ref = oracle.cn_count(off, dst, 2)
     G = accx.Graph.from_csr(off, dst, validate=validate)

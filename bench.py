@@ -619,18 +619,25 @@ def run_batch(args, S, stream):
     gen_s = time.perf_counter() - t0
     if S is None:
         S, _ = sched.default_scheduler()
-    model = S.model(True)
     sp = stream.cuda_stream
     total_m = sum(G.m for G in gs)
+    # the union first: the scheduler's plan is tuned on it (mode and bitmap offset
+    # by whole counts of the union), and both sides then count with that model
+    B = accx.Batch(gs)
+    U = B.union
+    U.relabel(stream=sp)
+    pl = S.plan(U, tune=True, stream=sp)
+    orient = pl["orient"]
+    model = S.model(orient)
     # one call sequence per graph (each graph relabeled and counted on its own)
     for G in gs:
         G.relabel(stream=sp)
-        G.set_model(model, orient=True)
+        G.set_model(model, orient=orient)
     torch.cuda.synchronize()
 
     def per_graph_step():
         for G in gs:
-            G.count(policy="model", out=None, stream=sp, orient=True)
+            G.count(policy="model", out=None, stream=sp, orient=orient)
             G.scan(0.3, 4, want_sim=False, want_label=False, want_cluster=False, stream=sp)
 
     for _ in range(args.warmup):
@@ -641,13 +648,9 @@ def run_batch(args, S, stream):
         per_graph_step()
     torch.cuda.synchronize()
     per_ms = (time.perf_counter() - t0) / args.steps * 1e3
-    # one union, autotuned shape, captured count + one query
-    B = accx.Batch(gs)
-    U = B.union
-    U.relabel(stream=sp)
-    U.set_model(model, orient=True)
-    kw, tune_ms, tune_all = U.autotune(policy="model", reps=2, stream=sp, orient=True)
-    B.capture(policy="model", stream=sp, orient=True, **kw)
+    # the union: autotuned shape, captured count + one query
+    kw, tune_ms, tune_all = U.autotune(policy="model", reps=2, stream=sp, orient=orient)
+    B.capture(policy="model", stream=sp, orient=orient, **kw)
     for _ in range(args.warmup):
         B.launch(stream=sp)
         U.scan(0.3, 4, want_sim=False, want_label=False, want_cluster=False, stream=sp)
@@ -675,6 +678,7 @@ def run_batch(args, S, stream):
            "per_graph": {"ms_per_step": round(per_ms, 3), "value": round(total_m / (per_ms / 1e3) / 1e9, 4)},
            "speedup_vs_per_graph": round(per_ms / step_ms, 3),
            "bit_exact": not bad, "checked_graphs": len(gs), "mismatched_graphs": bad[:8],
+           "plan": {k: pl[k] for k in ("orient", "bitmap_offset", "calibrated_offset", "mode_ms") if k in pl},
            "autotune": {"chosen": kw, "ms": round(tune_ms, 3), "all_ms": [round(x, 3) for x in tune_all]},
            "gpu_launches_per_step": "one captured CUDA graph (the count) + one SCAN query"}
     B.free()

@@ -72,6 +72,9 @@ __device__ __forceinline__ int accx_edge_kind(int policy, const uint8_t *table, 
 // work_u; merge / gallop list slots are reserved with one device atomic per list
 // and block (a CTA scan of the threads' counts).
 #define CL_EPT 8
+// partner ranges of galloping entries carry this flag in their length (the
+// bitmap kernel skips them); prefix lengths stay below 2^31 on a symmetric CSR
+#define OR_SL_GALLOP 0x80000000u
 struct cl_stats {
   unsigned long long e[ACCX_NUM_KINDS] = {0, 0, 0}, w[ACCX_NUM_KINDS] = {0, 0, 0}, o[ACCX_NUM_KINDS] = {0, 0, 0};
   __device__ __forceinline__ void add(int kind, uint32_t dv, uint32_t du) {
@@ -155,20 +158,22 @@ __global__ void __launch_bounds__(256, 4) k_classify(const uint32_t *__restrict_
         }
         uint32_t bwork = dv;
         if (ORIENT) {
-          // oriented bitmap entries: the partner's prefix start and its length cut
-          // at min(u, v), stored for the bitmap kernel's rounds
+          // oriented bitmap and galloping entries: the partner's prefix start and
+          // its length cut at min(u, v) (galloping ones flagged in the top bit),
+          // written where they are read: every entry of a row the bitmap kernel
+          // walks (zero for the other kinds), and every galloping entry
           uint2 sl = make_uint2(0u, 0u);
-          if (kind == ACCX_KIND_BITMAP) {
+          if (kind == ACCX_KIND_BITMAP || kind == ACCX_KIND_GALLOP) {
             const uint32_t sst = __ldg(off + v);
             uint32_t tt = sst + dv;
             if (v > u) {  // cut P(v) at u: u's position in N(v) is the reverse entry
               const uint32_t r = __ldg(rev + e);
               tt = (r >= sst && r < tt) ? r : sst;
             }
-            sl = make_uint2(sst, tt - sst);
+            sl = make_uint2(sst, (tt - sst) | (kind == ACCX_KIND_GALLOP ? OR_SL_GALLOP : 0u));
             bwork = tt - sst;
           }
-          or_sl[e] = sl;
+          if ((u < bm_idlim && du <= bm_pcap) || kind == ACCX_KIND_GALLOP) or_sl[e] = sl;
         }
         st.add(kind, dv, du);
         cm += kind == ACCX_KIND_MERGE;
@@ -858,7 +863,7 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s)
     k_merge_or<<<sms * 8, MERGE_WARPS * 32, 0, s>>>(off, dst, g->d_pre, g->d_rev, g->d_edge_list, list_cap, ctr,
                                                     cnt);
     ACCX_MARK(2);
-    k_gallop_or<GALLOP_OR_GROUP><<<sms * 8, MERGE_WARPS * 32, 0, s>>>(off, dst, g->d_pre, g->d_rev, g->d_edge_list, list_cap, ctr,
+    k_gallop_or<GALLOP_OR_GROUP><<<sms * 8, MERGE_WARPS * 32, 0, s>>>(off, dst, g->d_pre, g->d_or_sl, g->d_edge_list, list_cap, ctr,
                                                      cnt);
     ACCX_MARK(3);
     // the instance whose per-round arrays fit the block: 256 threads (four CTAs per

@@ -106,12 +106,16 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32) k_merge_or(const uint32_t *_
 // in order and binary-search each in the owner's prefix; every round starts at
 // the position the group's last lane reached.  Galloping edges mostly have
 // short partner lists (the low-degree owners outside the bitmap window), so a
-// warp works on 32/G edges at once.
+// warp works on 32/G edges at once.  The partner range comes from classify
+// (sl[e], already cut at min(x, y)), so an edge needs its list record, that
+// range and the owner's offset and prefix length: y < x exactly when e lies in
+// x's prefix, and then the owner's range is cut at e and the edge's credit goes
+// to e; otherwise to the end of the partner range (x's position in N(y)).
 template <int G>
 __global__ void __launch_bounds__(MERGE_WARPS * 32) k_gallop_or(const uint32_t *__restrict__ off,
                                                                  const int32_t *__restrict__ dst,
                                                                  const uint32_t *__restrict__ pre,
-                                                                 const uint32_t *__restrict__ rev,
+                                                                 const uint2 *__restrict__ sl,
                                                                  const uint2 *__restrict__ list, uint32_t list_cap,
                                                                  unsigned long long *__restrict__ ctr,
                                                                  int32_t *__restrict__ cnt) {
@@ -126,9 +130,10 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32) k_gallop_or(const uint32_t *
   for (unsigned long long it = ((unsigned long long)blockIdx.x * MERGE_WARPS + w) * (32 / G) + sub; it < total;
        it += ng) {
     const uint2 p = list[list_cap - 1 - it];
-    const uint32_t x = p.x, e = p.y, y = (uint32_t)__ldg(dst + e);
-    uint32_t xb, xe, yb, ye;
-    accx_or_ranges(off, pre, rev, x, y, e, &xb, &xe, &yb, &ye);
+    const uint32_t x = p.x, e = p.y;
+    const uint2 r = __ldg(sl + e);
+    const uint32_t xb = __ldg(off + x), xp = xb + __ldg(pre + x);
+    const uint32_t xe = min(xp, e), yb = r.x, ye = r.x + (r.y & ~OR_SL_GALLOP);
     uint32_t c = 0, lo = xb;
     for (uint32_t j0 = yb; j0 < ye && lo < xe; j0 += G) {
       const uint32_t j = j0 + (uint32_t)gl;
@@ -147,7 +152,7 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32) k_gallop_or(const uint32_t *
     }
 #pragma unroll
     for (int d = G / 2; d >= 1; d >>= 1) c += __shfl_xor_sync(gmask, c, d, G);
-    if (gl == 0 && c) atomicAdd(cnt + (y < x ? e : ye), (int32_t)c);  // the edge's prefix entry
+    if (gl == 0 && c) atomicAdd(cnt + (e < xp ? e : ye), (int32_t)c);  // the edge's prefix entry
     if (gl == 0) found += c;
   }
   if (gl == 0 && found) atomicAdd(&ctr[C_MATCH + ACCX_KIND_GALLOP], found);
@@ -275,7 +280,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bitmap_or(const uint32_t *__r
       if (k < pb) {
         const uint2 e = sl[k];
         sst = e.x;
-        len = e.y;
+        len = (e.y & OR_SL_GALLOP) ? 0u : e.y;  // galloping entries are not this kernel's
       }
       probed += len;
       const bool is_short = len > 0 && len < LONG_SEG, is_long = len >= LONG_SEG;

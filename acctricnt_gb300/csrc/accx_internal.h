@@ -149,7 +149,9 @@ int accx_rev_by_sort(accx_graph *g, const uint32_t *off, const uint32_t *tilerow
                      cudaStream_t s, uint32_t **rev_out);
 
 // Relabeled counts -> the handle's entry order (relabel.cu).
-int accx_relabel_gather(accx_graph *g, cudaStream_t s);
+int accx_relabel_gather(accx_graph *g, int32_t *host, cudaStream_t s);
+// The device address of pinned (mapped) host memory, or nullptr (graph.cu).
+void *accx_mapped_host(const void *p);
 
 int accx_build_csr_from_keys(accx_graph *g, unsigned long long *d_keys, uint64_t nkeys, uint32_t n,
                              cudaStream_t s);

@@ -95,7 +95,8 @@ __global__ void __launch_bounds__(256, 4) k_classify(const uint32_t *__restrict_
                                                   uint32_t list_cap, unsigned long long *__restrict__ work_u,
                                                   unsigned long long *__restrict__ ctr, const uint32_t *__restrict__ pre,
                                                   uint32_t bm_idlim, uint32_t bm_pcap, uint2 *__restrict__ or_sl,
-                                                  const uint32_t *__restrict__ rev) {
+                                                  const uint32_t *__restrict__ rev, int32_t *__restrict__ fill,
+                                                  int32_t bias) {
   static_assert(256 % CL_EPT == 0, "chunks inside tile-row tiles");
   __shared__ uint8_t s_table[ACCX_NB * ACCX_NB];
   __shared__ uint32_t s_wc[2][8];              // per-warp merge / gallop entries of the block
@@ -118,6 +119,15 @@ __global__ void __launch_bounds__(256, 4) k_classify(const uint32_t *__restrict_
     uint32_t cm = 0, cg = 0;       // this thread's merge / gallop entries
     uint32_t run_u = 0xffffffffu;  // the current row's bitmap work
     unsigned long long run_w = 0;
+    if (fill && e0 < e1) {  // oriented counts start every entry at the bias
+      if (e1 - e0 == CL_EPT) {
+        const int4 b4 = make_int4(bias, bias, bias, bias);
+        reinterpret_cast<int4 *>(fill + e0)[0] = b4;  // e0 is a multiple of 8: 32-byte aligned
+        reinterpret_cast<int4 *>(fill + e0)[1] = b4;
+      } else {
+        for (uint32_t e = e0; e < e1; e++) fill[e] = bias;
+      }
+    }
     if (e0 < e1) {
       // the partners and their sizes first (independent loads in flight)
       uint32_t vv[CL_EPT], dd[CL_EPT];
@@ -749,7 +759,10 @@ static unsigned classify_grid(int sms, uint32_t m) {
   return (unsigned)(blocks < g ? (blocks ? blocks : 1) : g);
 }
 
-static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s) {
+// host_out (optional): the caller's output as a device-mapped pointer; a count
+// on the relabeled CSR then writes it in its final gather (*host_done = true).
+static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s, int32_t *host_out = nullptr,
+                        bool *host_done = nullptr) {
   const uint32_t n = g->n, m = (uint32_t)g->m;
   int policy = o ? o->policy : ACCX_POLICY_HEURISTIC;
   int32_t bias = o ? o->bias : 0;
@@ -822,7 +835,6 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s)
         ACCX_CUDA_TRY(accx_dev_alloc((void **)&g->d_or_items, sizeof(uint32_t) * (size_t)items_cap, g->home));
       if (g->home) ACCX_CUDA_TRY(cudaStreamSynchronize(g->home));
     }
-    k_fill<<<sms * 8, 256, 0, s>>>(cnt, m, bias);
     k_pre<<<sms * 8, 256, 0, s>>>(off, dst, n, g->d_pre);
     // reverse entries: built on the first oriented count of this CSR and kept
     // (an index of the graph, like the tile rows).  The original CSR's comes
@@ -854,7 +866,8 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s)
       g->rev_csr = off;
     }
     k_classify<true><<<classify_grid(sms, m), 256, 0, s>>>(off, tilerow, dst, n, m, policy, g->d_table, g->d_edge_list,
-                                                          list_cap, work_u, ctr, g->d_pre, W, pcap, g->d_or_sl, g->d_rev);
+                                                          list_cap, work_u, ctr, g->d_pre, W, pcap, g->d_or_sl, g->d_rev,
+                                                          cnt, bias);  // classify also fills cnt with the bias
     k_item_counts<<<sms * 4, 256, 0, s>>>(off, dst, n, work_u, W, 1, target, g->d_icnt, ctr, g->d_pre);
     ACCX_CUDA_TRY(cub::DeviceScan::ExclusiveSum(g->d_scan_tmp, g->scan_tmp_bytes, g->d_icnt, g->d_prefix,
                                                 (int64_t)n + 1, s));
@@ -885,7 +898,8 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s)
     k_combine_or<<<tiles, 256, 0, s>>>(m, g->d_rev, cnt);
   } else {
     k_classify<false><<<classify_grid(sms, m), 256, 0, s>>>(off, tilerow, dst, n, m, policy, g->d_table, g->d_edge_list,
-                                                           list_cap, work_u, ctr, nullptr, 0u, 0u, nullptr, nullptr);
+                                                           list_cap, work_u, ctr, nullptr, 0u, 0u, nullptr, nullptr,
+                                                           nullptr, 0);
     const uint32_t W = (uint32_t)dkb * 8192u;        // dense ids (bits)
     const uint32_t S = (uint32_t)skb * 1024u / 8u;   // sparse 8-byte slots
     const size_t smem = (size_t)W / 8u + (size_t)S * 8u;
@@ -908,8 +922,9 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s)
     k_mirror<256><<<tiles, 256, 0, s>>>(off, tilerow, dst, n, m, bias, cnt);
   }
   if (rel) {
-    rc = accx_relabel_gather(g, s);
+    rc = accx_relabel_gather(g, host_out, s);
     if (rc) return rc;
+    if (host_out && host_done) *host_done = true;
   }
   ACCX_MARK(5);
 #undef ACCX_MARK
@@ -926,12 +941,18 @@ extern "C" int accx_cn_count(accx_graph *g, const accx_count_opts *opts, int32_t
   if (!g) return ACCX_ERR_INVALID_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   ACCX_CUDA_TRY(cudaSetDevice(g->device));
-  int rc = launch_count(g, opts, s);
+  // pinned host output, 16-byte aligned: written by the count's last pass itself
+  int32_t *mapped = out ? static_cast<int32_t *>(accx_mapped_host(out)) : nullptr;
+  if (mapped && ((uintptr_t)mapped & 15)) mapped = nullptr;
+  bool done = false;
+  int rc = launch_count(g, opts, s, mapped, &done);
   if (rc) {
     g->cnt_valid = false;
     return rc;
   }
-  if (out) {
+  if (out && done) {
+    ACCX_CUDA_TRY(cudaStreamSynchronize(s));
+  } else if (out) {
     rc = accx_copy_out(out, g->d_cnt, sizeof(int32_t) * (size_t)g->m, s);
     if (rc) return rc;
   }

@@ -131,6 +131,8 @@ static void *mapped_host(const void *p) {
   return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
 
+void *accx_mapped_host(const void *p) { return mapped_host(p); }
+
 static cudaError_t copy_via_kernel(void *d, const void *sp, size_t bytes, cudaStream_t s) {
   const size_t n16 = bytes / 16, head = n16 * 16;
   if (n16) {

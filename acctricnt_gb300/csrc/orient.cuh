@@ -447,12 +447,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bitmap_or(const uint32_t *__r
 }
 
 // Every credit lands on an edge's prefix entry (the entry in the larger id's
-// list), which starts at the bias; the other entry copies it.
-__global__ void k_fill(int32_t *__restrict__ cnt, uint32_t m, int32_t v) {
-  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < m; e += gridDim.x * blockDim.x) cnt[e] = v;
-}
-
-// One thread per entry: a suffix entry e = (v,u), u > v, takes the count of its
+// list), which starts at the bias (written by classify); the other entry copies
+// it.  One thread per entry: a suffix entry e = (v,u), u > v, takes the count of its
 // reverse rev[e] > e (u's prefix entry); entries without a reverse (asymmetric
 // input) keep the bias.
 __global__ void k_combine_or(uint32_t m, const uint32_t *__restrict__ rev, int32_t *__restrict__ cnt) {

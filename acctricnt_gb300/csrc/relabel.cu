@@ -141,8 +141,11 @@ __global__ void k_put_range(const uint32_t *__restrict__ key, const uint32_t *__
 
 // Four entries per thread and step, their index loads and then their gathers
 // issued together: the gathers are random reads, bound by latency at one a thread.
+// host (optional): the caller's pinned output buffer mapped into the device's
+// address space, written in the same pass (each warp store is 128 contiguous
+// bytes over the host link), which spares a separate copy of the counts.
 __global__ void k_gather_counts(const int32_t *__restrict__ cnt_r, const uint32_t *__restrict__ map, uint32_t m,
-                                int32_t *__restrict__ cnt) {
+                                int32_t *__restrict__ cnt, int32_t *__restrict__ host) {
   const uint32_t stride = gridDim.x * blockDim.x;
   uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
   for (; e + 3 * stride < m; e += 4 * stride) {
@@ -153,14 +156,24 @@ __global__ void k_gather_counts(const int32_t *__restrict__ cnt_r, const uint32_
     cnt[e + stride] = y;
     cnt[e + 2 * stride] = z;
     cnt[e + 3 * stride] = w;
+    if (host) {
+      host[e] = x;
+      host[e + stride] = y;
+      host[e + 2 * stride] = z;
+      host[e + 3 * stride] = w;
+    }
   }
-  for (; e < m; e += stride) cnt[e] = __ldg(cnt_r + __ldg(map + e));
+  for (; e < m; e += stride) {
+    const int32_t x = __ldg(cnt_r + __ldg(map + e));
+    cnt[e] = x;
+    if (host) host[e] = x;
+  }
 }
 
-int accx_relabel_gather(accx_graph *g, cudaStream_t s) {
+int accx_relabel_gather(accx_graph *g, int32_t *host, cudaStream_t s) {
   const uint32_t m = (uint32_t)g->m;
   if (!m) return ACCX_OK;
-  k_gather_counts<<<accx_sm_count(g->device) * 8, 256, 0, s>>>(g->d_rcnt, g->d_rmap, m, g->d_cnt);
+  k_gather_counts<<<accx_sm_count(g->device) * 8, 256, 0, s>>>(g->d_rcnt, g->d_rmap, m, g->d_cnt, host);
   ACCX_CUDA_TRY(cudaGetLastError());
   return ACCX_OK;
 }

@@ -502,9 +502,10 @@ def run_gb300(args):
             "matches": ({"found": matches[0], "bitmap_probed": matches[1]} if matches else None),
             "scan": scan, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             # this library's kernels per count: model inference (model policy); direct: classify, item
-            # counts, merge, gallop, bitmap, mirror; oriented: fill, prefix lengths, classify, item
-            # counts, item fill, merge, gallop, bitmap, combine; gather back (relabeled graph)
-            "gpu_launches": ((1 if policy == "model" else 0) + (9 if orient else 6) + 1) * args.steps,
+            # counts, merge, gallop, bitmap, mirror; oriented: prefix lengths, classify (which also
+            # writes the bias), item counts, item fill, merge, gallop, bitmap, combine; gather back
+            # (relabeled graph)
+            "gpu_launches": ((1 if policy == "model" else 0) + (8 if orient else 6) + 1) * args.steps,
             "clocks": clk.summary(),
             "sched": dict(sched_info, **(judged or {}))}
     G.free()

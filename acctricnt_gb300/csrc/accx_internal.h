@@ -74,6 +74,7 @@ struct accx_graph {
   unsigned long long *d_icnt = nullptr;    // n+1 bitmap items per owner
   unsigned long long *d_prefix = nullptr;  // n+1 exclusive prefix of d_icnt
   uint32_t *d_pre = nullptr;               // n prefix lengths (neighbours with smaller ids), oriented counts
+  uint2 *d_vinfo = nullptr;                // n (offset, prefix length) of the counting CSR, oriented counts
   uint2 *d_or_sl = nullptr;                // m oriented bitmap entries: (partner prefix start, cut length), 0 length = not bitmap
   uint32_t *d_or_items = nullptr;          // n + m/32 + 1 oriented bitmap work items: owner of each
   uint32_t *d_rev = nullptr;               // m reverse entry of every entry of the counting CSR (oriented counts)

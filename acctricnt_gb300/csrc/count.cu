@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(256, 4) k_classify(const uint32_t *__restrict_
                                                   unsigned long long *__restrict__ ctr, const uint32_t *__restrict__ pre,
                                                   uint32_t bm_idlim, uint32_t bm_pcap, uint2 *__restrict__ or_sl,
                                                   const uint32_t *__restrict__ rev, int32_t *__restrict__ fill,
-                                                  int32_t bias) {
+                                                  int32_t bias, const uint2 *__restrict__ vinfo) {
   static_assert(256 % CL_EPT == 0, "chunks inside tile-row tiles");
   __shared__ uint8_t s_table[ACCX_NB * ACCX_NB];
   __shared__ uint32_t s_wc[2][8];              // per-warp merge / gallop entries of the block
@@ -130,11 +130,21 @@ __global__ void __launch_bounds__(256, 4) k_classify(const uint32_t *__restrict_
     }
     if (e0 < e1) {
       // the partners and their sizes first (independent loads in flight)
-      uint32_t vv[CL_EPT], dd[CL_EPT];
+      // (oriented: the partner's offset and prefix length from one 8-byte record)
+      uint32_t vv[CL_EPT], dd[CL_EPT], ss[CL_EPT];
 #pragma unroll
       for (int j = 0; j < CL_EPT; j++) vv[j] = e0 + j < e1 ? (uint32_t)__ldg(dst + e0 + j) : 0u;
 #pragma unroll
-      for (int j = 0; j < CL_EPT; j++) dd[j] = ORIENT ? __ldg(pre + vv[j]) : __ldg(off + vv[j] + 1) - __ldg(off + vv[j]);
+      for (int j = 0; j < CL_EPT; j++) {
+        if (ORIENT) {
+          const uint2 vi = __ldg(vinfo + vv[j]);
+          ss[j] = vi.x;
+          dd[j] = vi.y;
+        } else {
+          ss[j] = 0;
+          dd[j] = __ldg(off + vv[j] + 1) - __ldg(off + vv[j]);
+        }
+      }
       const uint32_t t = e0 / 256u;
       uint32_t u = accx_row_of(off, __ldg(tilerow + t), __ldg(tilerow + t + 1) + 1, e0);
       uint32_t rb = __ldg(off + u), re = __ldg(off + u + 1);
@@ -174,7 +184,7 @@ __global__ void __launch_bounds__(256, 4) k_classify(const uint32_t *__restrict_
           // walks (zero for the other kinds), and every galloping entry
           uint2 sl = make_uint2(0u, 0u);
           if (kind == ACCX_KIND_BITMAP || kind == ACCX_KIND_GALLOP) {
-            const uint32_t sst = __ldg(off + v);
+            const uint32_t sst = ss[j];
             uint32_t tt = sst + dv;
             if (v > u) {  // cut P(v) at u: u's position in N(v) is the reverse entry
               const uint32_t r = __ldg(rev + e);
@@ -726,7 +736,7 @@ int accx_prefix_lengths(accx_graph *g, cudaStream_t s) {
   if (rc) return rc;
   const bool rel = g->d_roff != nullptr;
   if (g->n) k_pre<<<accx_sm_count(g->device) * 8, 256, 0, s>>>(rel ? g->d_roff : g->d_off, rel ? g->d_rdst : g->d_dst,
-                                                                g->n, g->d_pre);
+                                                                g->n, g->d_pre, nullptr);
   ACCX_CUDA_TRY(cudaGetLastError());
   return ACCX_OK;
 }
@@ -829,13 +839,14 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s,
     // per-entry bitmap work and the item array (n + m/32 + 1 bounds the items:
     // an owner is cut into at most max(1, degree/32) slices)
     const uint32_t items_cap = n + m / 32u + 1u;
-    if (!g->d_or_sl || !g->d_or_items) {
+    if (!g->d_or_sl || !g->d_or_items || !g->d_vinfo) {
       if (!g->d_or_sl) ACCX_CUDA_TRY(accx_dev_alloc((void **)&g->d_or_sl, sizeof(uint2) * (size_t)m, g->home));
+      if (!g->d_vinfo) ACCX_CUDA_TRY(accx_dev_alloc((void **)&g->d_vinfo, sizeof(uint2) * (size_t)n, g->home));
       if (!g->d_or_items)
         ACCX_CUDA_TRY(accx_dev_alloc((void **)&g->d_or_items, sizeof(uint32_t) * (size_t)items_cap, g->home));
       if (g->home) ACCX_CUDA_TRY(cudaStreamSynchronize(g->home));
     }
-    k_pre<<<sms * 8, 256, 0, s>>>(off, dst, n, g->d_pre);
+    k_pre<<<sms * 8, 256, 0, s>>>(off, dst, n, g->d_pre, g->d_vinfo);
     // reverse entries: built on the first oriented count of this CSR and kept
     // (an index of the graph, like the tile rows).  The original CSR's comes
     // from validation; a known-symmetric CSR's from the sort (accx_rev_by_sort);
@@ -867,7 +878,7 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s,
     }
     k_classify<true><<<classify_grid(sms, m), 256, 0, s>>>(off, tilerow, dst, n, m, policy, g->d_table, g->d_edge_list,
                                                           list_cap, work_u, ctr, g->d_pre, W, pcap, g->d_or_sl, g->d_rev,
-                                                          cnt, bias);  // classify also fills cnt with the bias
+                                                          cnt, bias, g->d_vinfo);  // classify also fills cnt with the bias
     k_item_counts<<<sms * 4, 256, 0, s>>>(off, dst, n, work_u, W, 1, target, g->d_icnt, ctr, g->d_pre);
     ACCX_CUDA_TRY(cub::DeviceScan::ExclusiveSum(g->d_scan_tmp, g->scan_tmp_bytes, g->d_icnt, g->d_prefix,
                                                 (int64_t)n + 1, s));
@@ -876,7 +887,7 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s,
     k_merge_or<<<sms * 8, MERGE_WARPS * 32, 0, s>>>(off, dst, g->d_pre, g->d_rev, g->d_edge_list, list_cap, ctr,
                                                     cnt);
     ACCX_MARK(2);
-    k_gallop_or<GALLOP_OR_GROUP><<<sms * 8, MERGE_WARPS * 32, 0, s>>>(off, dst, g->d_pre, g->d_or_sl, g->d_edge_list, list_cap, ctr,
+    k_gallop_or<GALLOP_OR_GROUP><<<sms * 8, MERGE_WARPS * 32, 0, s>>>(g->d_vinfo, dst, g->d_or_sl, g->d_edge_list, list_cap, ctr,
                                                      cnt);
     ACCX_MARK(3);
     // the instance whose per-round arrays fit the block: 256 threads (four CTAs per
@@ -899,7 +910,7 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s,
   } else {
     k_classify<false><<<classify_grid(sms, m), 256, 0, s>>>(off, tilerow, dst, n, m, policy, g->d_table, g->d_edge_list,
                                                            list_cap, work_u, ctr, nullptr, 0u, 0u, nullptr, nullptr,
-                                                           nullptr, 0);
+                                                           nullptr, 0, nullptr);
     const uint32_t W = (uint32_t)dkb * 8192u;        // dense ids (bits)
     const uint32_t S = (uint32_t)skb * 1024u / 8u;   // sparse 8-byte slots
     const size_t smem = (size_t)W / 8u + (size_t)S * 8u;

@@ -595,7 +595,7 @@ extern "C" int accx_graph_free(accx_graph *g) {
   if (!g) return ACCX_ERR_INVALID_ARG;
   void *ptrs[] = {g->d_off,      g->d_dst,    g->d_cnt,  g->d_edge_list, g->d_icnt,  g->d_prefix, g->d_scan_tmp,
                   g->d_counters, g->d_table,  g->d_roff, g->d_rdst,      g->d_rmap,  g->d_rcnt,   g->d_oldid,
-                  g->d_newid,    g->d_simkey, g->d_tilerow, g->d_rtilerow, g->d_src, g->d_pre, g->d_or_sl, g->d_or_items, g->d_rev, g->d_rev_orig};
+                  g->d_newid,    g->d_simkey, g->d_tilerow, g->d_rtilerow, g->d_src, g->d_pre, g->d_or_sl, g->d_or_items, g->d_rev, g->d_rev_orig, g->d_vinfo};
   accx_query_ctx_release(&g->qc);
   for (void *p : ptrs) accx_dev_free(p, g->home);
   for (int i = 0; i <= ACCX_NUM_PHASES; i++)

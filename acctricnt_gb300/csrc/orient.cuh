@@ -23,12 +23,16 @@
 // scale 24, 8 measured 4% slower
 #define LONG_UNROLL 16
 
-// pre[u] = |N(u) ∩ [0, u)|.
+// pre[u] = |N(u) ∩ [0, u)|; vinfo (optional) = (off[u], pre[u]) packed, so that a
+// kernel looking up a random partner reads one 8-byte record instead of two arrays
+// (on graphs without locality, e.g. Erdos-Renyi, each lookup is a DRAM access).
 __global__ void k_pre(const uint32_t *__restrict__ off, const int32_t *__restrict__ dst, uint32_t n,
-                      uint32_t *__restrict__ pre) {
+                      uint32_t *__restrict__ pre, uint2 *__restrict__ vinfo) {
   for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
     const uint32_t b = __ldg(off + u), e = __ldg(off + u + 1);
-    pre[u] = accx_lower_bound(dst, b, e, (int32_t)u) - b;
+    const uint32_t p = accx_lower_bound(dst, b, e, (int32_t)u) - b;
+    pre[u] = p;
+    if (vinfo) vinfo[u] = make_uint2(b, p);
   }
 }
 
@@ -108,13 +112,12 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32) k_merge_or(const uint32_t *_
 // short partner lists (the low-degree owners outside the bitmap window), so a
 // warp works on 32/G edges at once.  The partner range comes from classify
 // (sl[e], already cut at min(x, y)), so an edge needs its list record, that
-// range and the owner's offset and prefix length: y < x exactly when e lies in
+// range and the owner's offset and prefix length (vinfo): y < x exactly when e lies in
 // x's prefix, and then the owner's range is cut at e and the edge's credit goes
 // to e; otherwise to the end of the partner range (x's position in N(y)).
 template <int G>
-__global__ void __launch_bounds__(MERGE_WARPS * 32) k_gallop_or(const uint32_t *__restrict__ off,
+__global__ void __launch_bounds__(MERGE_WARPS * 32) k_gallop_or(const uint2 *__restrict__ vinfo,
                                                                  const int32_t *__restrict__ dst,
-                                                                 const uint32_t *__restrict__ pre,
                                                                  const uint2 *__restrict__ sl,
                                                                  const uint2 *__restrict__ list, uint32_t list_cap,
                                                                  unsigned long long *__restrict__ ctr,
@@ -131,8 +134,8 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32) k_gallop_or(const uint32_t *
        it += ng) {
     const uint2 p = list[list_cap - 1 - it];
     const uint32_t x = p.x, e = p.y;
-    const uint2 r = __ldg(sl + e);
-    const uint32_t xb = __ldg(off + x), xp = xb + __ldg(pre + x);
+    const uint2 r = __ldg(sl + e), xi = __ldg(vinfo + x);
+    const uint32_t xb = xi.x, xp = xi.x + xi.y;
     const uint32_t xe = min(xp, e), yb = r.x, ye = r.x + (r.y & ~OR_SL_GALLOP);
     uint32_t c = 0, lo = xb;
     for (uint32_t j0 = yb; j0 < ye && lo < xe; j0 += G) {

@@ -482,7 +482,14 @@ def run_gb300(args):
                 "merge_equiv_bytes": int(4 * float(np.sum(np.diff(G.download()[0]).astype(np.float64) ** 2)) + 4 * G.m)}
     e2e = None
     if not args.no_e2e and rank == 0:
-        e2e = measure_e2e(G, policy, 5, S, orient)
+        # the end-to-end leg plans with the scheduler file as trained (its calibrated
+        # offsets), not with the offset just tuned on this graph
+        from acctricnt_gb300 import sched as _sched
+        S_file = accx.Scheduler.load(_sched.DEFAULT_PATH) if S is not None else None
+        e2e = measure_e2e(G, policy, 5, S_file, orient)
+        if S_file is not None:
+            e2e["scheduler"] = "the scheduler file as trained (untuned plan)"
+            S_file.free()
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
         off, dst = G.download()

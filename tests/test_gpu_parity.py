@@ -320,6 +320,28 @@ def test_reverse_index_sources_give_the_same_counts(validate):
     G.free()
 
 
+@pytest.mark.parametrize("shift", [0, 1])
+def test_counts_into_pinned_host_memory(shift):
+    """A count into pinned host memory: written by the relabeled count's final
+    gather when the buffer is 16-byte aligned (shift 0), through the copy
+    otherwise (shift 1 entry); the same counts as into pageable memory, and the
+    resident counts stay valid for queries."""
+    torch = pytest.importorskip("torch")
+    off, dst = accx.generate_host(accx.rmat_params(15, 16, seed=9))
+    ref = oracle.cn_count(off, dst, 2)
+    G = accx.Graph.from_csr(off, dst)
+    G.relabel()
+    buf = torch.full((len(dst) + 4,), -7, dtype=torch.int32).pin_memory()
+    for orient in (True, False):
+        buf.fill_(-7)
+        G.count(policy="bitmap", bias=2, out=buf.data_ptr() + 4 * shift, orient=orient)
+        got = buf.numpy()
+        assert np.array_equal(got[shift:shift + len(dst)], ref), orient
+        assert np.all(got[:shift] == -7) and np.all(got[shift + len(dst):] == -7)
+        assert np.array_equal(G.read_counts(), ref)
+    G.free()
+
+
 def test_query_before_count_is_not_ready():
     off, dst = accx.generate_host(accx.rmat_params(8, 8))
     G = accx.Graph.from_csr(off, dst)

@@ -834,7 +834,8 @@ static int launch_count(accx_graph *g, const accx_count_opts *o, cudaStream_t s,
   if (orient) {
     const uint32_t W = (uint32_t)dkb * 8192u;       // dense ids (bits); bitmap owners have ids below W
     const uint32_t pcap = (uint32_t)skb * 256u;     // owner-prefix counters
-    const size_t smem = (size_t)W / 8u + 16u + (size_t)pcap * 4u + (size_t)W / 16u;  // + the zero word, padded
+    // words + the zero word (padded), owner counters + 32 spares, word ranks
+    const size_t smem = (size_t)W / 8u + 16u + ((size_t)pcap + 32u) * 4u + (size_t)W / 16u;
     const uint32_t target = ITEM_TARGET_DEFAULT;
     // per-entry bitmap work and the item array (n + m/32 + 1 bounds the items:
     // an owner is cut into at most max(1, degree/32) slices)

@@ -198,10 +198,11 @@ __device__ __forceinline__ uint32_t or_piece(const int32_t *__restrict__ dst, ui
     const uint32_t id = min((uint32_t)((r & 1) ? v[r >> 1].y : v[r >> 1].x), W);  // W: the zero word
     const uint32_t wd = words[id >> 5];
     if ((wd >> (id & 31u)) & 1u) {
-      const uint32_t rk = wbase[id >> 5] + __popc(wd & ((1u << (id & 31u)) - 1u));
+      // the rank: the word's base plus the set bits up to and including this one, less one
+      const uint32_t rk = wbase[id >> 5] + __popc(wd << (~id & 31u)) - 1u;
       h++;
       atomicAdd(cl + 64u * (r >> 1) + (uint32_t)(r & 1), 1);
-      if (rk < pxs) atomicAdd(&ocnt[rk], 1u);  // always true on a sorted CSR
+      atomicAdd(&ocnt[rk], 1u);  // rk < pxs on a sorted CSR, < pxs + 31 always (spare counters)
     }
   }
   return h;
@@ -241,8 +242,10 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bitmap_or(const uint32_t *__r
   extern __shared__ __align__(16) uint32_t smem[];
   const uint32_t nwords = W / 32;
   uint32_t *words = smem;                                          // nwords + a zero word (ids >= W probe it)
-  uint32_t *ocnt = smem + nwords + 4;                              // pcap owner-prefix counters
-  uint16_t *wbase = reinterpret_cast<uint16_t *>(ocnt + pcap);     // nwords first-id positions
+  // pcap owner-prefix counters + 32 spares: a found id's rank is at most a word's
+  // base (< pxs) + 31, so the counter add needs no bounds test even on unsorted input
+  uint32_t *ocnt = smem + nwords + 4;
+  uint16_t *wbase = reinterpret_cast<uint16_t *>(ocnt + pcap + 32);  // nwords first-id positions
   __shared__ unsigned long long s_it;
   __shared__ uint32_t s_tot, s_nseg, s_nlong, s_next;
   __shared__ uint32_t s_wsum[32], s_wcnt[32], s_wlong[32];
@@ -377,9 +380,9 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bitmap_or(const uint32_t *__r
             const uint32_t id = min((uint32_t)xs[r], W);
             const uint32_t wd = words[id >> 5];
             if ((wd >> (id & 31u)) & 1u) {
-              const uint32_t rk = wbase[id >> 5] + __popc(wd & ((1u << (id & 31u)) - 1u));
+              const uint32_t rk = wbase[id >> 5] + __popc(wd << (~id & 31u)) - 1u;
               atomicAdd(cnt + gi[r], 1);
-              if (rk < pxs) atomicAdd(&ocnt[rk], 1u);  // always true on a sorted CSR
+              atomicAdd(&ocnt[rk], 1u);  // rk < pxs on a sorted CSR, < pxs + 31 always (spare counters)
               atomicAdd(&s_hit[sg[r]], 1u);
             }
           }

@@ -1,5 +1,5 @@
 """Learned kernel scheduler from Python: the library's scheduler (accx_sched,
-csrc/sched.cpp) plus numpy helpers that judge a schedule against measured
+csrc/sched.cpp) plus numpy helpers that assess a schedule against measured
 per-bucket timings.
 
 Training data, training, whole-count calibration of the bitmap kind's offset,

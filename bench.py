@@ -266,7 +266,7 @@ def measure_e2e(G, policy, reps, sched=None, orient=False):
                                               "/".join(sorted(modes)))}
 
 
-# Fixed single policies a scheduled count is judged against: the reference's
+# Fixed single policies a scheduled count is compared with: the reference's
 # ratio-50 rule ("plain") and each kernel kind for every edge, in both modes.
 # The direct merge kind for every edge is left out: on these graphs the ratio-50
 # rule already merges nearly every edge (the same work), and on 1M-degree hubs
@@ -288,7 +288,7 @@ def time_fixed_policies(G, steps, stream, world, slow_ms=1500.0):
     return out
 
 
-def judge_schedule(G, S, ms, orient, fixed, stream, world, steps):
+def compare_schedule(G, S, ms, orient, fixed, stream, world, steps):
     """The scheduled count against the fixed policies and against the per-bucket
     best table: measured regret, the other mode under its own model, and the
     additive per-bucket estimate from buckets timed alone."""
@@ -312,7 +312,7 @@ def judge_schedule(G, S, ms, orient, fixed, stream, world, steps):
             "regret": measured_regret(ms, dict(fixed, per_bucket_best_table=best_ms)),
             "bucket_regret_isolated": {k: round(v, 4) for k, v in r.items()},
             "kinds_chosen": {k: int((mt.reshape(-1)[e > 0] == i).sum()) for i, k in enumerate(accx.KIND_NAMES)},
-            "judge_s": round(time.perf_counter() - t0, 2)}
+            "compare_s": round(time.perf_counter() - t0, 2)}
 
 
 CPU_STRIPES = 20  # a whole CPU count = this many stripes of CheckCoreBitmap's entry chunks
@@ -445,11 +445,11 @@ def run_gb300(args):
     # line, so fewer steps (each count takes seconds)
     plain_ms, plain_phases = time_counts(G, "heuristic", None, min(args.steps, 3), 1, stream, world)
     plain_ms = max_over_ranks(plain_ms, world)
-    judged = None
+    compared = None
     if S is not None and args.regret and rank == 0:
         fixed = time_fixed_policies(G, max(1, args.steps // 2), stream, world)
         fixed["direct_heuristic"] = round(plain_ms, 3)
-        judged = judge_schedule(G, S, ms, orient, fixed, stream, world, max(1, args.steps // 2))
+        compared = compare_schedule(G, S, ms, orient, fixed, stream, world, max(1, args.steps // 2))
     total_m = sum_over_ranks(G.m, world)
     value = total_m / (ms / 1e3) / 1e9
     plain_value = total_m / (plain_ms / 1e3) / 1e9
@@ -514,7 +514,7 @@ def run_gb300(args):
             # (relabeled graph)
             "gpu_launches": ((1 if policy == "model" else 0) + (8 if orient else 6) + 1) * args.steps,
             "clocks": clk.summary(),
-            "sched": dict(sched_info, **(judged or {}))}
+            "sched": dict(sched_info, **(compared or {}))}
     G.free()
     del G
     if not args.no_extras and rank == 0 and world == 1:
@@ -602,11 +602,11 @@ def run_skew(args, S, stream):
         deg = np.diff(G.download()[0].astype(np.int64))
         del a, b
         fixed = time_fixed_policies(G, steps, stream, 1)
-        judged = judge_schedule(G, S, ms, orient, fixed, stream, 1, steps)
+        compared = compare_schedule(G, S, ms, orient, fixed, stream, 1, steps)
         out[name] = {"n": G.n, "m": G.m, "max_degree": int(deg.max()), "gen_s": round(gen_s, 2),
                      "relabel_ms": round(relabel_ms, 2), "plan": pl, "ms_per_step": round(ms, 3), "steps": steps,
                      "value": round(G.m / (ms / 1e3) / 1e9, 4), "phases_ms": {k: round(v, 3) for k, v in phases.items()},
-                     "bit_exact": exact, **judged}
+                     "bit_exact": exact, **compared}
         G.free()
         del G
     out["bit_exact"] = all(v["bit_exact"] for v in out.values() if isinstance(v, dict))

@@ -1,7 +1,7 @@
 """The learned scheduler: the cost model's own CUDA forward/backward kernels
 against a float64 CPU restatement, training, register-resident inference, the
 model policy's counts (bit-exact), and its gain over the reference heuristic
-judged by exhaustive per-bucket timing on a graph it was not trained on."""
+assessed by exhaustive per-bucket timing on a graph it was not trained on."""
 import numpy as np
 import pytest
 

@@ -79,3 +79,32 @@ def test_no_device_status():
     with pytest.raises(accx.AccxError) as ei:
         accx.Graph.from_csr(off, dst)
     assert ei.value.status in (accx.ERR_NO_DEVICE, accx.ERR_CUDA)
+
+
+def test_scheduler_rejects_too_many_candidates():
+    """Checked before any device work."""
+    with pytest.raises(accx.AccxError) as ei:
+        accx.Scheduler.train(candidates=accx.SCHED_MAX_CANDIDATES + 1)
+    assert ei.value.status == accx.ERR_INVALID_ARG
+
+
+def _sched_text(version, with_candidates):
+    model = "0 " * accx.MODEL_NPARAMS
+    info = "info 100 10 1 -1 1 1 1 0 " + "1 " * accx.SCHED_NOFFSETS
+    if with_candidates:
+        info += "3 1 " + "1 " * accx.SCHED_MAX_CANDIDATES
+    body = "".join("model %d 0 0 -1\n%s\n%s\n" % (o, model, info) for o in (0, 1))
+    return "accx-sched %d\n%s" % (version, body)
+
+
+@pytest.mark.parametrize("text", [_sched_text(3, True), _sched_text(2, False), "accx-sched 2\nmodel 1 0 0 0\n",
+                                  "not a scheduler file\n"])
+def test_malformed_scheduler_files_are_rejected(tmp_path, text):
+    """Unknown versions, a version-2 file without its candidates record, models
+    out of order and foreign files: an I/O status, found while parsing (before
+    any model reaches the device)."""
+    p = tmp_path / "bad.model"
+    p.write_text(text)
+    with pytest.raises(accx.AccxError) as ei:
+        accx.Scheduler.load(str(p))
+    assert ei.value.status == accx.ERR_IO
